@@ -1,0 +1,280 @@
+/*
+ * tecto.h - C ABI of the GB300 (sm_103a) engine for the plate-tectonics simulation step.
+ *
+ * This is the only boundary between callers and the engine: plain C types, plain pointers
+ * and sizes, explicit CUDA streams (passed as opaque pointers), integer status codes.
+ * Nothing here exits the process; every call returns TECTO_OK (0) or a negative code.
+ *
+ * Each entry point names the reference interface it replaces (MarWo22/master_thesis,
+ * paths relative to the project root).
+ *
+ * Threading: one world per handle.  Calls on different worlds may run concurrently from
+ * different host threads; calls on the same world must be serialised by the caller.
+ * Device work is enqueued on the stream given; a NULL stream means the legacy default stream.
+ */
+#ifndef TECTO_H
+#define TECTO_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TECTO_MAX_PLATES 255          /* MAX_PLATE_COUNT, src/cuda_compute/plate_tectonics_kernel.cuh:13 */
+#define TECTO_NUM_PAIRS 32385         /* 255*254/2, NUM_TRIANGLE_ENTRIES, plate_tectonic_sim.h:25 */
+#define TECTO_NUM_DIV_WORDS 1013      /* NUM_WORDS_TRIANGLE_SINGLE_BITS, plate_tectonic_sim.h:30 */
+#define TECTO_MAX_VORONOI_GENS 8
+
+/* ---- status codes ------------------------------------------------------------------ */
+#define TECTO_OK 0
+#define TECTO_ERR_INVALID (-1)        /* bad argument (null handle, size out of range, ...) */
+#define TECTO_ERR_CUDA (-2)           /* a CUDA runtime call failed; see tecto_last_error_string */
+#define TECTO_ERR_OOM (-3)            /* device allocation failed */
+#define TECTO_ERR_DEVICE_TIMEOUT (-4) /* a bounded device-side wait gave up (error flag set) */
+#define TECTO_ERR_UNSUPPORTED (-5)    /* configuration the engine does not implement */
+#define TECTO_ERR_BUDGET (-6)         /* admission refused: memory budget exhausted */
+
+typedef struct CUstream_st *tecto_stream_t; /* same type as cudaStream_t */
+typedef struct tecto_world tecto_world;
+
+/* ---- settings ---------------------------------------------------------------------- */
+
+/* Field-for-field mirror of KernelSettings (src/cuda_compute/kernel_settings.cuh:4-81): same
+ * names, same order, same 4-byte types, so a KernelSettings object can be copied in bytewise.
+ * Defaults come from tecto_settings_default(). */
+typedef struct tecto_kernel_settings {
+    float inelasticCollisionMultiplierContinental;
+    float inelasticCollisionMultiplierSubduction;
+    float inelasticCollisionMultiplierAccretion;
+    float frictionCoefficientContinental;
+    float frictionCoefficientSubduction;
+    float frictionCoefficientAccretion;
+    float environmentalDragCoefficient;
+    float velocitySmoothingFactor;
+    float directionSmoothingFactor;
+    float breakScoreSmoothingFactor;
+    float mergeDotDirectionThreshold;
+    float mergeVelocityDiffThreshold;
+    float mergeMinVelocity;
+    int mergeWaitAfterSplit;
+    int minPlateSize;
+    float continentalCrustThreshold;
+    float divergence_height_target_min;
+    float divergence_height_target_max;
+    float divergence_interpolation_factor;
+    int collisionTypeUpdateCooldown;
+    int minCollisionSize;
+    float subductionOverUpliftMultiplier;
+    float subductionUnderUpliftMultiplier;
+    float continentalUpliftMultiplier;
+    float minUpliftClamp;
+    float maxUpliftClamp;
+    int upliftRange;
+    int subductionOverRange;
+    int continentalPropMaxIters;
+    float continentalPropThreshold;
+    float hydrationPipeCrossSection;
+    float hydrationPipeLength;
+    float hydrationRainfall;
+    float hydrationEvaporation;
+    float gravity;
+    float sedimentCapacity;
+    float sedimentErosionRate;
+    float sedimentDepositionRate;
+    float pressureAccumulation;
+    float pressureDecayRate;
+    int pressureBlurRange;
+    float pressureMultiplier;
+    float curlNoiseMultiplier;
+    float stressSplitThreshold;
+    int targetMinimumPlateArea;
+    int targetMaximumPlateArea;
+    float thermalErosionStrength;
+    float thermalErosionAmplitude;
+    float thermalCellSize;
+    float thermalThresholdAngle;
+} tecto_kernel_settings;
+
+/* SimulationSettings (src/generation_settings.h:67-76); the std::vector of Voronoi generation
+ * sizes becomes a fixed array plus a count. */
+typedef struct tecto_simulation_settings {
+    int numStartingPlates;
+    uint32_t seed;
+    int numVoronoiSeeds[TECTO_MAX_VORONOI_GENS];
+    int numVoronoiGenerations;
+    int iterationsForCCL;
+} tecto_simulation_settings;
+
+/* Uplift modes. */
+#define TECTO_UPLIFT_GAUSSIAN 0  /* +upliftAmount on convergent cells, separable Gaussian blur */
+#define TECTO_UPLIFT_NONE 1      /* no uplift phase */
+
+/* CCL connectivity modes. */
+#define TECTO_CCL_4 4
+#define TECTO_CCL_8 8
+#define TECTO_CCL_REF8 9 /* the union set of src/cuda_compute/ccl.cu:90-177 */
+
+/* Knobs the reference hard-codes (plate_tectonic_sim.cu:73, :336-363) or does not have. */
+typedef struct tecto_step_settings {
+    int hydraulicIterations;  /* reference: 10 (literal loop bound, plate_tectonic_sim.cu:336) */
+    float hydraulicDt;        /* reference: 1.0 (literal, plate_tectonic_sim.cu:338-363) */
+    int thermalIterations;    /* reference: 1 (single launch, plate_tectonic_sim.cu:73) */
+    int upliftMode;           /* TECTO_UPLIFT_* */
+    float upliftAmount;       /* added on convergent cells before the blur */
+    float upliftSigma;        /* Gaussian sigma in cells */
+    int upliftRadius;         /* taps on each side (<= 8) */
+    int cclConnectivity;      /* TECTO_CCL_* */
+    int sortRadixBits;        /* 0 = autotuned; else 6..8 */
+    int reserved[7];
+} tecto_step_settings;
+
+typedef struct tecto_settings {
+    tecto_kernel_settings kernel;
+    tecto_simulation_settings sim;
+    tecto_step_settings step;
+} tecto_settings;
+
+/* Reference defaults: KernelSettings initialisers (kernel_settings.cuh:6-71), SimulationSettings
+ * initialisers (generation_settings.h:69-72), and the reference's literal step constants. */
+int tecto_settings_default(tecto_settings *out);
+
+/* The synthetic benchmark parameterisation: rain 0.01, evaporation 0.05, Kc 0.1, Ks 0.3, Kd 0.1,
+ * dt 0.02, 20 hydraulic and 10 thermal iterations, talus 0.01, rate 0.5, Gaussian uplift 0.01 with
+ * sigma 1.5 radius 3, continental threshold 0, 4-connected CCL every 10 steps.  Everything else
+ * keeps the reference default. */
+int tecto_settings_baseline(tecto_settings *out);
+
+/* Parse a config.json (src/config.h:23-33 keys "heightmap_dimensions" {x,y} and "use_renderer",
+ * plus optional "kernel_settings", "simulation_settings" and "step_settings" objects whose keys are
+ * the field names above) on top of *inout.  width/height receive heightmap_dimensions when present
+ * (may be NULL). */
+int tecto_settings_from_json(const char *json_text, tecto_settings *inout, int *width, int *height);
+
+/* ---- per-plate kinematics ---------------------------------------------------------- */
+
+/* The hot-path subset of PlateData (src/cuda_compute/types/plate_data.h:5-38). */
+typedef struct tecto_plate {
+    float velocity;      /* PlateData::velocity (cells per step) */
+    float direction_x;   /* PlateData::direction */
+    float direction_y;
+    float pixelCenter_x; /* PlateData::pixelCenter, sub-cell position in [0,1) */
+    float pixelCenter_y;
+} tecto_plate;
+
+/* ---- fields ------------------------------------------------------------------------ */
+#define TECTO_FIELD_HEIGHT 0       /* f32[W*H]  m_heightMapTexture */
+#define TECTO_FIELD_WATER 1        /* f32[W*H]  m_hydrationLevel */
+#define TECTO_FIELD_SEDIMENT 2     /* f32[W*H]  m_sedimentLevel */
+#define TECTO_FIELD_FLUX 3         /* f32x4[W*H] m_hydrationFlux (left, +y, right, -y) */
+#define TECTO_FIELD_PLATE_ID 4     /* u8[W*H]   m_plateIdsTexture */
+#define TECTO_FIELD_LABELS 5       /* u32[W*H]  CCL labels (minimum linear index per component) */
+#define TECTO_FIELD_COLLISION 6    /* u32[W*H]  packed arrival word of the last step (m_plateCollisions) */
+#define TECTO_FIELD_TYPE_BITMAP 7  /* u8[32385] m_collisionTypeBitmap */
+#define TECTO_FIELD_DIV_BITMAP 8   /* u32[1013] m_divergenceBitmap */
+#define TECTO_FIELD_SORT_KEYS 9    /* u32[W*H]  destination cells of the last step, sorted */
+#define TECTO_FIELD_SORT_VALS 10   /* u32[W*H]  source cells, in the same order */
+#define TECTO_FIELD_ACCRETION 11   /* u8[W*H]   accretion marks of the last resolve (0 = none) */
+#define TECTO_FIELD_COUNT 12
+
+/* ---- world lifecycle (replaces PlateTectonicSim, plate_tectonic_sim.h:110-130) ------ */
+
+/* PlateTectonicSim::PlateTectonicSim(width, height, seed, interop) + initializeTextures()
+ * (plate_tectonic_sim.cu:28-36, :844-872): allocates the world's device state (zeroed) on the
+ * current device and uploads settings (the reference never uploads them headless).  Also loads
+ * the reference's seed convention: the step's noise seed is seed + iteration. */
+int tecto_world_create(const tecto_settings *settings, int width, int height, uint32_t seed,
+                       tecto_world **out);
+int tecto_world_destroy(tecto_world *world);
+
+/* Replace the settings of a live world (Gui::simulationSettingsSection ->
+ * copyHostKernelSettingsToDevice, kernel_settings.cu:7-9, gui.cpp:435-441). */
+int tecto_world_set_settings(tecto_world *world, const tecto_settings *settings);
+int tecto_world_get_settings(const tecto_world *world, tecto_settings *out);
+int tecto_world_size(const tecto_world *world, int *width, int *height);
+
+/* Synthetic world generator (host-only, needs no GPU): numPlates plates from a toroidal Voronoi
+ * of numPlates uniform seed points, per-plate velocity vector uniform in [-velRange, velRange]^2,
+ * half the plates continental (0.5 + N(0, 0.05)) and half oceanic (-0.5 + N(0, 0.02)), water,
+ * sediment and flux zero.  Deterministic in genSeed on every platform.  Any output may be NULL. */
+int tecto_generate_world_host(int width, int height, int numPlates, float velRange, uint64_t genSeed,
+                              float *height_out, uint8_t *plate_id_out, tecto_plate *plates_out);
+
+/* PlateTectonicSim::initialize (plate_tectonic_sim.cu:40-51) for the synthetic generator above:
+ * generates on the host, uploads, resets water/sediment/flux/bitmaps and the iteration count. */
+int tecto_world_init_synthetic(tecto_world *world, int numPlates, float velRange, uint64_t genSeed,
+                               tecto_stream_t stream);
+
+/* Host <-> device copies of one field (synchronous w.r.t. the stream: the call returns after
+ * the copy completed).  bytes must equal the field's size. */
+int tecto_world_upload(tecto_world *world, int field, const void *host, size_t bytes,
+                       tecto_stream_t stream);
+int tecto_world_download(tecto_world *world, int field, void *host, size_t bytes,
+                         tecto_stream_t stream);
+/* Borrow the device pointer of a field (valid until the next call that steps the world). */
+int tecto_world_field(tecto_world *world, int field, void **device_ptr, size_t *bytes);
+
+int tecto_world_set_plates(tecto_world *world, const tecto_plate *plates, int count,
+                           tecto_stream_t stream);
+int tecto_world_get_plates(tecto_world *world, tecto_plate *plates, int count,
+                           tecto_stream_t stream);
+int tecto_world_set_iteration(tecto_world *world, uint32_t iteration);
+int tecto_world_get_iteration(const tecto_world *world, uint32_t *iteration);
+
+/* ---- stepping ---------------------------------------------------------------------- */
+
+/* PlateTectonicSim::executeIteration (plate_tectonic_sim.cu:54-131), hot-path phases only:
+ * plate offsets, advection + radix sort + segmented winner pick, collision typing, resolve,
+ * uplift, thermal, hydraulic, accretion, CCL every iterationsForCCL steps, plate sub-cell
+ * centre update.  Asynchronous on `stream`; nSteps steps are enqueued (as a CUDA graph once
+ * warm). */
+int tecto_world_step(tecto_world *world, int nSteps, tecto_stream_t stream);
+
+/* Phase entry points (each a subset of executeIteration, for parity tests and custom drivers).
+ * Calling them in the order below is equivalent to one tecto_world_step. */
+
+/* getPlateCollisions (plate_tectonic_sim.cu:174-208) + determineCollisionType kernel and
+ * createCollisionTypeMatrix (:232-241): plate offsets, advection, sort on destination, collision
+ * words, collision-type evidence and the pair bitmap update. */
+int tecto_phase_collide(tecto_world *world, tecto_stream_t stream);
+/* processCollisions + flipDivergedBitmap (:246-262) and the uplift phase of upliftMode. */
+int tecto_phase_resolve(tecto_world *world, tecto_stream_t stream);
+/* thermalErosionKernel (:73), `iterations` deterministic gather iterations. */
+int tecto_phase_thermal(tecto_world *world, int iterations, tecto_stream_t stream);
+/* applyHydraulicErosion (:331-373) with `iterations` sub-iterations of step dt. */
+int tecto_phase_hydraulic(tecto_world *world, int iterations, float dt, tecto_stream_t stream);
+/* applyAccretion (:90-93) and the plate sub-cell centre update of applyPlateMovementChanges
+ * (plate_tectonics_kernel.cu:1871-1878); advances the iteration counter. */
+int tecto_phase_finish(tecto_world *world, tecto_stream_t stream);
+/* applyCCL's labelling part (plate_tectonic_sim.cu:375-389): labels of equal-plate components
+ * on the torus, each the minimum linear index of its component. */
+int tecto_phase_ccl(tecto_world *world, int connectivity, tecto_stream_t stream);
+
+/* Standalone stable LSD radix sort of (u32 key, u32 value) pairs on the device: the sort that
+ * replaces registerPlateCollisions' atomic slotting (plate_tectonics_kernel.cu:273-298).
+ * Keys must be < 2^key_bits.  scratch must hold tecto_sort_scratch_bytes(n, key_bits) bytes.
+ * Result in keys_out/vals_out; inputs are not modified. */
+size_t tecto_sort_scratch_bytes(size_t n, int key_bits);
+int tecto_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_out,
+                     uint32_t *vals_out, size_t n, int key_bits, void *scratch,
+                     size_t scratch_bytes, tecto_stream_t stream);
+
+/* ---- status -------------------------------------------------------------------------- */
+
+/* Number of engine kernels enqueued for this world so far (graph replays count the kernels of the
+ * captured step); the reference has no counterpart (it prints a per-step wall time,
+ * plate_tectonic_sim.cu:128-130). */
+int tecto_world_launch_count(const tecto_world *world, uint64_t *count);
+
+/* Wait for the world's stream work and report device-side error flags (bounded waits that gave
+ * up) as TECTO_ERR_DEVICE_TIMEOUT. */
+int tecto_world_check(tecto_world *world, tecto_stream_t stream);
+const char *tecto_last_error_string(void);
+const char *tecto_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TECTO_H */

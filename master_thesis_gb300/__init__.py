@@ -1,0 +1,369 @@
+"""master_thesis_gb300 - GB300 (sm_103a) engine for the plate-tectonics simulation step.
+
+Python binding of the C ABI in include/tecto.h (libtecto.so, built in-tree by _build.py).  The
+engine itself is CUDA; this module only loads the library, mirrors its structs with ctypes and
+offers a thin `World` wrapper.  There is no CPU fallback: if libtecto.so is missing or cannot be
+loaded, `lib()` raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import os
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "libtecto.so"
+
+TECTO_OK = 0
+ERRORS = {
+    -1: "TECTO_ERR_INVALID",
+    -2: "TECTO_ERR_CUDA",
+    -3: "TECTO_ERR_OOM",
+    -4: "TECTO_ERR_DEVICE_TIMEOUT",
+    -5: "TECTO_ERR_UNSUPPORTED",
+    -6: "TECTO_ERR_BUDGET",
+}
+MAX_PLATES = 255
+NUM_PAIRS = 32385
+NUM_DIV_WORDS = 1013
+
+UPLIFT_GAUSSIAN, UPLIFT_NONE = 0, 1
+CCL_4, CCL_8, CCL_REF8 = 4, 8, 9
+
+(FIELD_HEIGHT, FIELD_WATER, FIELD_SEDIMENT, FIELD_FLUX, FIELD_PLATE_ID, FIELD_LABELS,
+ FIELD_COLLISION, FIELD_TYPE_BITMAP, FIELD_DIV_BITMAP, FIELD_SORT_KEYS, FIELD_SORT_VALS,
+ FIELD_ACCRETION) = range(12)
+
+KERNEL_FIELDS = [
+    ("inelasticCollisionMultiplierContinental", C.c_float),
+    ("inelasticCollisionMultiplierSubduction", C.c_float),
+    ("inelasticCollisionMultiplierAccretion", C.c_float),
+    ("frictionCoefficientContinental", C.c_float),
+    ("frictionCoefficientSubduction", C.c_float),
+    ("frictionCoefficientAccretion", C.c_float),
+    ("environmentalDragCoefficient", C.c_float),
+    ("velocitySmoothingFactor", C.c_float),
+    ("directionSmoothingFactor", C.c_float),
+    ("breakScoreSmoothingFactor", C.c_float),
+    ("mergeDotDirectionThreshold", C.c_float),
+    ("mergeVelocityDiffThreshold", C.c_float),
+    ("mergeMinVelocity", C.c_float),
+    ("mergeWaitAfterSplit", C.c_int),
+    ("minPlateSize", C.c_int),
+    ("continentalCrustThreshold", C.c_float),
+    ("divergence_height_target_min", C.c_float),
+    ("divergence_height_target_max", C.c_float),
+    ("divergence_interpolation_factor", C.c_float),
+    ("collisionTypeUpdateCooldown", C.c_int),
+    ("minCollisionSize", C.c_int),
+    ("subductionOverUpliftMultiplier", C.c_float),
+    ("subductionUnderUpliftMultiplier", C.c_float),
+    ("continentalUpliftMultiplier", C.c_float),
+    ("minUpliftClamp", C.c_float),
+    ("maxUpliftClamp", C.c_float),
+    ("upliftRange", C.c_int),
+    ("subductionOverRange", C.c_int),
+    ("continentalPropMaxIters", C.c_int),
+    ("continentalPropThreshold", C.c_float),
+    ("hydrationPipeCrossSection", C.c_float),
+    ("hydrationPipeLength", C.c_float),
+    ("hydrationRainfall", C.c_float),
+    ("hydrationEvaporation", C.c_float),
+    ("gravity", C.c_float),
+    ("sedimentCapacity", C.c_float),
+    ("sedimentErosionRate", C.c_float),
+    ("sedimentDepositionRate", C.c_float),
+    ("pressureAccumulation", C.c_float),
+    ("pressureDecayRate", C.c_float),
+    ("pressureBlurRange", C.c_int),
+    ("pressureMultiplier", C.c_float),
+    ("curlNoiseMultiplier", C.c_float),
+    ("stressSplitThreshold", C.c_float),
+    ("targetMinimumPlateArea", C.c_int),
+    ("targetMaximumPlateArea", C.c_int),
+    ("thermalErosionStrength", C.c_float),
+    ("thermalErosionAmplitude", C.c_float),
+    ("thermalCellSize", C.c_float),
+    ("thermalThresholdAngle", C.c_float),
+]
+
+
+class KernelSettings(C.Structure):
+    """tecto_kernel_settings: field-for-field mirror of the reference's KernelSettings."""
+    _fields_ = KERNEL_FIELDS
+
+
+class SimulationSettings(C.Structure):
+    _fields_ = [
+        ("numStartingPlates", C.c_int),
+        ("seed", C.c_uint32),
+        ("numVoronoiSeeds", C.c_int * 8),
+        ("numVoronoiGenerations", C.c_int),
+        ("iterationsForCCL", C.c_int),
+    ]
+
+
+class StepSettings(C.Structure):
+    _fields_ = [
+        ("hydraulicIterations", C.c_int),
+        ("hydraulicDt", C.c_float),
+        ("thermalIterations", C.c_int),
+        ("upliftMode", C.c_int),
+        ("upliftAmount", C.c_float),
+        ("upliftSigma", C.c_float),
+        ("upliftRadius", C.c_int),
+        ("cclConnectivity", C.c_int),
+        ("sortRadixBits", C.c_int),
+        ("reserved", C.c_int * 7),
+    ]
+
+
+class Settings(C.Structure):
+    _fields_ = [("kernel", KernelSettings), ("sim", SimulationSettings), ("step", StepSettings)]
+
+    def copy(self) -> "Settings":
+        s = Settings()
+        C.memmove(C.byref(s), C.byref(self), C.sizeof(Settings))
+        return s
+
+
+class Plate(C.Structure):
+    _fields_ = [
+        ("velocity", C.c_float),
+        ("direction_x", C.c_float),
+        ("direction_y", C.c_float),
+        ("pixelCenter_x", C.c_float),
+        ("pixelCenter_y", C.c_float),
+    ]
+
+
+PLATE_DTYPE = np.dtype(
+    [("velocity", "<f4"), ("direction_x", "<f4"), ("direction_y", "<f4"),
+     ("pixelCenter_x", "<f4"), ("pixelCenter_y", "<f4")]
+)
+
+_lib = None
+
+
+class TectoError(RuntimeError):
+    def __init__(self, code: int, where: str, msg: str = ""):
+        super().__init__(f"{where}: {ERRORS.get(code, code)} {msg}")
+        self.code = code
+
+
+def _declare(L: C.CDLL) -> None:
+    P = C.c_void_p
+    sig = {
+        "tecto_settings_default": ([C.POINTER(Settings)], C.c_int),
+        "tecto_settings_baseline": ([C.POINTER(Settings)], C.c_int),
+        "tecto_settings_from_json": ([C.c_char_p, C.POINTER(Settings), C.POINTER(C.c_int), C.POINTER(C.c_int)], C.c_int),
+        "tecto_world_create": ([C.POINTER(Settings), C.c_int, C.c_int, C.c_uint32, C.POINTER(P)], C.c_int),
+        "tecto_world_destroy": ([P], C.c_int),
+        "tecto_world_set_settings": ([P, C.POINTER(Settings)], C.c_int),
+        "tecto_world_get_settings": ([P, C.POINTER(Settings)], C.c_int),
+        "tecto_world_size": ([P, C.POINTER(C.c_int), C.POINTER(C.c_int)], C.c_int),
+        "tecto_generate_world_host": ([C.c_int, C.c_int, C.c_int, C.c_float, C.c_uint64, P, P, P], C.c_int),
+        "tecto_world_init_synthetic": ([P, C.c_int, C.c_float, C.c_uint64, P], C.c_int),
+        "tecto_world_upload": ([P, C.c_int, P, C.c_size_t, P], C.c_int),
+        "tecto_world_download": ([P, C.c_int, P, C.c_size_t, P], C.c_int),
+        "tecto_world_field": ([P, C.c_int, C.POINTER(P), C.POINTER(C.c_size_t)], C.c_int),
+        "tecto_world_set_plates": ([P, P, C.c_int, P], C.c_int),
+        "tecto_world_get_plates": ([P, P, C.c_int, P], C.c_int),
+        "tecto_world_set_iteration": ([P, C.c_uint32], C.c_int),
+        "tecto_world_get_iteration": ([P, C.POINTER(C.c_uint32)], C.c_int),
+        "tecto_world_step": ([P, C.c_int, P], C.c_int),
+        "tecto_phase_collide": ([P, P], C.c_int),
+        "tecto_phase_resolve": ([P, P], C.c_int),
+        "tecto_phase_thermal": ([P, C.c_int, P], C.c_int),
+        "tecto_phase_hydraulic": ([P, C.c_int, C.c_float, P], C.c_int),
+        "tecto_phase_finish": ([P, P], C.c_int),
+        "tecto_phase_ccl": ([P, C.c_int, P], C.c_int),
+        "tecto_sort_scratch_bytes": ([C.c_size_t, C.c_int], C.c_size_t),
+        "tecto_sort_pairs": ([P, P, P, P, C.c_size_t, C.c_int, P, C.c_size_t, P], C.c_int),
+        "tecto_world_check": ([P, P], C.c_int),
+        "tecto_world_launch_count": ([P, C.POINTER(C.c_uint64)], C.c_int),
+        "tecto_last_error_string": ([], C.c_char_p),
+        "tecto_version": ([], C.c_char_p),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+
+
+def lib() -> C.CDLL:
+    """The loaded engine library.  Raises if it has not been built (no fallback exists)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(
+                f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`"
+            )
+        L = C.CDLL(str(LIB_PATH))
+        _declare(L)
+        _lib = L
+    return _lib
+
+
+def check(code: int, where: str) -> None:
+    if code != TECTO_OK:
+        raise TectoError(code, where, lib().tecto_last_error_string().decode(errors="replace"))
+
+
+def default_settings() -> Settings:
+    s = Settings()
+    check(lib().tecto_settings_default(C.byref(s)), "tecto_settings_default")
+    return s
+
+
+def baseline_settings() -> Settings:
+    s = Settings()
+    check(lib().tecto_settings_baseline(C.byref(s)), "tecto_settings_baseline")
+    return s
+
+
+def settings_from_json(text: str, base: Settings | None = None) -> tuple[Settings, int, int]:
+    s = (base or default_settings()).copy()
+    w, h = C.c_int(0), C.c_int(0)
+    check(lib().tecto_settings_from_json(text.encode(), C.byref(s), C.byref(w), C.byref(h)),
+          "tecto_settings_from_json")
+    return s, w.value, h.value
+
+
+def generate_world(W: int, H: int, plates: int, vel_range: float, gen_seed: int):
+    """Host-only synthetic world: (height f32[H,W], plate id u8[H,W], plates structured[255])."""
+    h = np.empty((H, W), np.float32)
+    ids = np.empty((H, W), np.uint8)
+    pl = np.zeros(MAX_PLATES, PLATE_DTYPE)
+    check(lib().tecto_generate_world_host(W, H, plates, vel_range, gen_seed, h.ctypes.data,
+                                          ids.ctypes.data, pl.ctypes.data), "tecto_generate_world_host")
+    return h, ids, pl
+
+
+_FIELD_DT = {
+    FIELD_HEIGHT: (np.float32, 1), FIELD_WATER: (np.float32, 1), FIELD_SEDIMENT: (np.float32, 1),
+    FIELD_FLUX: (np.float32, 4), FIELD_PLATE_ID: (np.uint8, 1), FIELD_LABELS: (np.uint32, 1),
+    FIELD_COLLISION: (np.uint32, 1), FIELD_SORT_KEYS: (np.uint32, 1), FIELD_SORT_VALS: (np.uint32, 1),
+    FIELD_ACCRETION: (np.uint8, 1),
+}
+
+
+def _stream(stream) -> int | None:
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    return int(getattr(stream, "cuda_stream", stream))
+
+
+class World:
+    """One simulated world on the current GPU (tecto_world)."""
+
+    def __init__(self, settings: Settings, W: int, H: int, seed: int = 1000):
+        self.W, self.H = W, H
+        p = C.c_void_p()
+        check(lib().tecto_world_create(C.byref(settings), W, H, seed, C.byref(p)), "tecto_world_create")
+        self.ptr = p
+
+    def close(self) -> None:
+        if getattr(self, "ptr", None):
+            lib().tecto_world_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def init_synthetic(self, plates: int, vel_range: float, gen_seed: int, stream=None) -> None:
+        check(lib().tecto_world_init_synthetic(self.ptr, plates, vel_range, gen_seed, _stream(stream)),
+              "tecto_world_init_synthetic")
+
+    def set_settings(self, s: Settings) -> None:
+        check(lib().tecto_world_set_settings(self.ptr, C.byref(s)), "tecto_world_set_settings")
+
+    def download(self, field: int, stream=None) -> np.ndarray:
+        if field == FIELD_TYPE_BITMAP:
+            out = np.empty(NUM_PAIRS, np.uint8)
+        elif field == FIELD_DIV_BITMAP:
+            out = np.empty(NUM_DIV_WORDS, np.uint32)
+        else:
+            dt, k = _FIELD_DT[field]
+            out = np.empty((self.H, self.W, k) if k > 1 else (self.H, self.W), dt)
+        check(lib().tecto_world_download(self.ptr, field, out.ctypes.data, out.nbytes, _stream(stream)),
+              "tecto_world_download")
+        return out
+
+    def upload(self, field: int, arr: np.ndarray, stream=None) -> None:
+        a = np.ascontiguousarray(arr)
+        check(lib().tecto_world_upload(self.ptr, field, a.ctypes.data, a.nbytes, _stream(stream)),
+              "tecto_world_upload")
+
+    def plates(self, stream=None) -> np.ndarray:
+        out = np.zeros(MAX_PLATES, PLATE_DTYPE)
+        check(lib().tecto_world_get_plates(self.ptr, out.ctypes.data, MAX_PLATES, _stream(stream)),
+              "tecto_world_get_plates")
+        return out
+
+    def set_plates(self, plates: np.ndarray, stream=None) -> None:
+        a = np.ascontiguousarray(plates, dtype=PLATE_DTYPE)
+        check(lib().tecto_world_set_plates(self.ptr, a.ctypes.data, len(a), _stream(stream)),
+              "tecto_world_set_plates")
+
+    @property
+    def iteration(self) -> int:
+        v = C.c_uint32()
+        check(lib().tecto_world_get_iteration(self.ptr, C.byref(v)), "tecto_world_get_iteration")
+        return v.value
+
+    @iteration.setter
+    def iteration(self, v: int) -> None:
+        check(lib().tecto_world_set_iteration(self.ptr, v), "tecto_world_set_iteration")
+
+    def step(self, n: int = 1, stream=None) -> None:
+        check(lib().tecto_world_step(self.ptr, n, _stream(stream)), "tecto_world_step")
+
+    def collide(self, stream=None):
+        check(lib().tecto_phase_collide(self.ptr, _stream(stream)), "tecto_phase_collide")
+
+    def resolve(self, stream=None):
+        check(lib().tecto_phase_resolve(self.ptr, _stream(stream)), "tecto_phase_resolve")
+
+    def thermal(self, iters: int, stream=None):
+        check(lib().tecto_phase_thermal(self.ptr, iters, _stream(stream)), "tecto_phase_thermal")
+
+    def hydraulic(self, iters: int, dt: float, stream=None):
+        check(lib().tecto_phase_hydraulic(self.ptr, iters, dt, _stream(stream)), "tecto_phase_hydraulic")
+
+    def finish(self, stream=None):
+        check(lib().tecto_phase_finish(self.ptr, _stream(stream)), "tecto_phase_finish")
+
+    def ccl(self, connectivity: int, stream=None):
+        check(lib().tecto_phase_ccl(self.ptr, connectivity, _stream(stream)), "tecto_phase_ccl")
+
+    @property
+    def launches(self) -> int:
+        v = C.c_uint64()
+        check(lib().tecto_world_launch_count(self.ptr, C.byref(v)), "tecto_world_launch_count")
+        return v.value
+
+    def check(self, stream=None):
+        check(lib().tecto_world_check(self.ptr, _stream(stream)), "tecto_world_check")
+
+
+def load_config(path: str | os.PathLike) -> tuple[Settings, int, int]:
+    """Read a reference-style config.json (plus optional settings objects)."""
+    return settings_from_json(Path(path).read_text())
+
+
+__all__ = [n for n in dir() if not n.startswith("_")]

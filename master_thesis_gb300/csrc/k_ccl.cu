@@ -1,0 +1,176 @@
+// k_ccl.cu - connected-component labelling of equal plate ids on the torus.
+//
+// Replaces the reference's union-find CCL (src/cuda_compute/ccl.cu:35-177, driver
+// plate_tectonic_sim.cu:375-389).  Labels converge to the minimum linear index of each
+// component, as the reference's roots do.  Three edge sets:
+//   TECTO_CCL_4    left, top;
+//   TECTO_CCL_8    left, top, top-left, top-right;
+//   TECTO_CCL_REF8 the reference kernels' union set: every cell links left and top-left when
+//                  equal, plus init's single link to the first equal of (tl, t, tr, l)
+//                  (ccl.cu:107-116), plus top and top-right on row 0 (ccl.cu:161-170).
+// (Edges are undirected; each is generated once, from the lower-right cell.)
+//
+// Three kernels: union-find inside a 32x16 tile in shared memory (roots = smallest index),
+// unions across tile borders with global atomicMin linking, and a flatten pass.
+#include "tecto_internal.cuh"
+
+namespace tecto {
+
+namespace {
+
+constexpr int CX = 32, CY = 16;
+
+// Edge mask of cell (x, y): bit 0 l, bit 1 t, bit 2 tl, bit 3 tr.
+__device__ __forceinline__ unsigned edge_mask(const uint8_t *id, int x, int y, int W, int H, int mode)
+{
+    const uint8_t c = id[(size_t)y * W + x];
+    const bool el = id[cidx(x - 1, y, W, H)] == c;
+    const bool et = id[cidx(x, y - 1, W, H)] == c;
+    const bool etl = id[cidx(x - 1, y - 1, W, H)] == c;
+    const bool etr = id[cidx(x + 1, y - 1, W, H)] == c;
+    if (mode == TECTO_CCL_4) return (el ? 1u : 0u) | (et ? 2u : 0u);
+    if (mode == TECTO_CCL_8) return (el ? 1u : 0u) | (et ? 2u : 0u) | (etl ? 4u : 0u) | (etr ? 8u : 0u);
+    unsigned m = (el ? 1u : 0u) | (etl ? 4u : 0u);
+    if (y == 0) {
+        m |= (et ? 2u : 0u) | (etr ? 8u : 0u);
+    } else if (!etl) {
+        if (et) m |= 2u;
+        else if (etr) m |= 8u;
+    }
+    return m;
+}
+
+__device__ __forceinline__ int smem_find(const int *par, int a)
+{
+    while (par[a] != a) a = par[a];
+    return a;
+}
+
+__device__ __forceinline__ void smem_union(int *par, int a, int b)
+{
+    while (true) {
+        a = smem_find(par, a);
+        b = smem_find(par, b);
+        if (a == b) return;
+        if (a > b) {
+            const int tmp = a;
+            a = b;
+            b = tmp;
+        }
+        const int old = atomicMin(par + b, a);
+        if (old == b) return;
+        b = old;
+    }
+}
+
+__device__ __forceinline__ uint32_t g_find(const uint32_t *L, uint32_t a)
+{
+    uint32_t p = L[a];
+    while (p != a) {
+        a = p;
+        p = L[a];
+    }
+    return a;
+}
+
+__device__ __forceinline__ void g_union(uint32_t *L, uint32_t a, uint32_t b)
+{
+    while (true) {
+        a = g_find(L, a);
+        b = g_find(L, b);
+        if (a == b) return;
+        if (a > b) {
+            const uint32_t tmp = a;
+            a = b;
+            b = tmp;
+        }
+        const uint32_t old = atomicMin(L + b, a);
+        if (old == b) return;
+        b = old;
+    }
+}
+
+__global__ __launch_bounds__(256) void k_ccl_local(const uint8_t *id, uint32_t *labels, int W, int H,
+                                                   int mode)
+{
+    __shared__ int par[CX * CY];
+    const int x0 = blockIdx.x * CX, y0 = blockIdx.y * CY;
+    const int tw = min(CX, W - x0), th = min(CY, H - y0);
+    for (int e = threadIdx.x; e < CX * CY; e += blockDim.x) par[e] = e;
+    __syncthreads();
+    const int dxs[4] = {-1, 0, -1, 1}, dys[4] = {0, -1, -1, -1};
+    for (int e = threadIdx.x; e < CX * CY; e += blockDim.x) {
+        const int ly = e / CX, lx = e - ly * CX;
+        if (lx >= tw || ly >= th) continue;
+        const int x = x0 + lx, y = y0 + ly;
+        const unsigned m = edge_mask(id, x, y, W, H, mode);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (!(m & (1u << k))) continue;
+            const int nx = wrapc(x + dxs[k], W), ny = wrapc(y + dys[k], H);
+            const int nlx = nx - x0, nly = ny - y0;
+            if (nlx >= 0 && nlx < tw && nly >= 0 && nly < th) smem_union(par, e, nly * CX + nlx);
+        }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < CX * CY; e += blockDim.x) {
+        const int ly = e / CX, lx = e - ly * CX;
+        if (lx >= tw || ly >= th) continue;
+        const int r = smem_find(par, e);
+        const int ry = r / CX, rx = r - ry * CX;
+        labels[(size_t)(y0 + ly) * W + x0 + lx] = (uint32_t)((y0 + ry) * W + x0 + rx);
+    }
+}
+
+// Unions across tile borders: only cells on a tile's top row or left/right column have edges
+// leaving the tile.
+__global__ __launch_bounds__(128) void k_ccl_border(const uint8_t *id, uint32_t *labels, int W, int H,
+                                                    int mode)
+{
+    const int x0 = blockIdx.x * CX, y0 = blockIdx.y * CY;
+    const int tw = min(CX, W - x0), th = min(CY, H - y0);
+    const int nb = tw + 2 * th;  // top row, left column, right column (corners repeat harmlessly)
+    const int dxs[4] = {-1, 0, -1, 1}, dys[4] = {0, -1, -1, -1};
+    for (int e = threadIdx.x; e < nb; e += blockDim.x) {
+        int lx, ly;
+        if (e < tw) { lx = e; ly = 0; }
+        else if (e < tw + th) { lx = 0; ly = e - tw; }
+        else { lx = tw - 1; ly = e - tw - th; }
+        const int x = x0 + lx, y = y0 + ly;
+        const unsigned m = edge_mask(id, x, y, W, H, mode);
+        for (int k = 0; k < 4; ++k) {
+            if (!(m & (1u << k))) continue;
+            const int nx = wrapc(x + dxs[k], W), ny = wrapc(y + dys[k], H);
+            const int nlx = nx - x0, nly = ny - y0;
+            if (nlx >= 0 && nlx < tw && nly >= 0 && nly < th) continue;  // handled locally
+            g_union(labels, (uint32_t)((size_t)y * W + x), (uint32_t)((size_t)ny * W + nx));
+        }
+    }
+}
+
+__global__ void k_ccl_flatten(uint32_t *labels, uint32_t n)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) labels[i] = g_find(labels, i);
+}
+
+}  // namespace
+
+int launch_ccl(tecto_world *w, int connectivity, cudaStream_t st)
+{
+    if (connectivity != TECTO_CCL_4 && connectivity != TECTO_CCL_8 && connectivity != TECTO_CCL_REF8) {
+        set_error("cclConnectivity must be 4, 8 or 9 (ref8)");
+        return TECTO_ERR_INVALID;
+    }
+    const dim3 grid((unsigned)((w->W + CX - 1) / CX), (unsigned)((w->H + CY - 1) / CY));
+    const uint8_t *id = w->b.id[w->cur_id];
+    k_ccl_local<<<grid, 256, 0, st>>>(id, w->b.labels, w->W, w->H, connectivity);
+    k_ccl_border<<<grid, 128, 0, st>>>(id, w->b.labels, w->W, w->H, connectivity);
+    const uint32_t n = (uint32_t)w->N;
+    k_ccl_flatten<<<(n + 255) / 256, 256, 0, st>>>(w->b.labels, n);
+    TECTO_CUDA(cudaGetLastError());
+    w->launches += 3;
+    return TECTO_OK;
+}
+
+}  // namespace tecto

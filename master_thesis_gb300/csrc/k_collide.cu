@@ -1,0 +1,203 @@
+// k_collide.cu - plate displacement, collision words from the sorted arrivals, collision-type
+// evidence and the plate-pair type bitmap.  Reference: src/cuda_compute/plate_tectonics_kernel.cu.
+#include "tecto_internal.cuh"
+
+namespace tecto {
+
+namespace {
+
+// Per-plate integer displacement (getPixelMovements, :248-257) and the sub-cell centre update
+// of applyPlateMovementChanges (:1871-1878).  Also resets the per-step counters.
+__global__ void k_plates(tecto_plate *plates, int2 *off, Control *ctl)
+{
+    const int k = threadIdx.x;
+    if (k < kPlates) {
+        tecto_plate p = plates[k];
+        const float mx = p.direction_x * p.velocity;
+        const float my = p.direction_y * p.velocity;
+        const float cx = p.pixelCenter_x + mx;
+        const float cy = p.pixelCenter_y + my;
+        const float fx = floorf(cx), fy = floorf(cy);
+        off[k] = make_int2((int)fx, (int)fy);
+        p.pixelCenter_x = cx - fx;
+        p.pixelCenter_y = cy - fy;
+        plates[k] = p;
+    } else if (k == kPlates) {
+        off[k] = make_int2(0, 0);
+    }
+    if (k == 0) ctl->acc_count = 0;
+}
+
+// writeCollision's classification (:794-836): returns category 0..4 or -1 to skip.  The early
+// exit is the as-compiled `(packed & 1) && ((packed >> 4) & (15 < cooldown))` (:813).
+__device__ __forceinline__ int evidence_category(const uint8_t *bm, uint8_t A, uint8_t B, float hA,
+                                                 float hB, float thr, int cooldown, uint32_t *pair)
+{
+    const bool cond = A < B;
+    const uint8_t mn = cond ? A : B, mx = cond ? B : A;
+    const float mnH = cond ? hA : hB, mxH = cond ? hB : hA;
+    const uint32_t idx = tri_index(mn, mx);
+    *pair = idx;
+    const uint32_t packed = __ldg(bm + idx);
+    if ((packed & 1u) && ((packed >> 4) & (uint32_t)(0x0F < cooldown))) return -1;
+    const bool minCont = mnH >= thr, maxCont = mxH >= thr;
+    if (minCont && maxCont) return 4;
+    if (minCont) return 2;
+    if (maxCont) return 0;
+    if (mnH <= mxH) return 1;
+    return 3;
+}
+
+// Segmented winner pick over the sorted (destination, source) pairs: the first position of
+// each destination's run builds the packed arrival word of registerPlateCollisions (:273-298)
+// from its first four sources (ascending source order), writes zero words into the gap of
+// destinations nobody moved into, and for convergent cells adds the collision-type evidence of
+// the determineCollisionType kernel (:838-888) with warp-aggregated atomics.
+__global__ __launch_bounds__(256) void k_words(const uint32_t *keys, const uint32_t *vals, uint32_t n,
+                                               uint32_t N, const uint8_t *id_old, const float *h_old,
+                                               const uint8_t *bm, PairCounts *counts, uint32_t *word,
+                                               float thr, int cooldown)
+{
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned lane = threadIdx.x & 31u;
+    const bool valid = j < n;
+    uint32_t key = 0;
+    bool leader = false;
+    uint8_t ids[4] = {0, 0, 0, 0};
+    float hs[4] = {0, 0, 0, 0};
+    int cnt = 0;
+    if (valid) {
+        key = keys[j];
+        const uint32_t prev = j > 0 ? keys[j - 1] : 0xffffffffu;
+        leader = j == 0 || prev != key;
+        if (leader) {
+            const uint32_t gap0 = j == 0 ? 0u : prev + 1u;
+            for (uint32_t c = gap0; c < key; ++c) word[c] = 0u;
+            uint32_t wv = 0;
+            for (int k = 0; k < 4; ++k) {
+                if (j + k >= n || keys[j + k] != key) break;
+                const uint32_t src = vals[j + k];
+                ids[k] = id_old[src];
+                hs[k] = h_old[src];  // determineCollisionHeight: height at the arrival's source
+                wv |= (uint32_t)(255u - ids[k]) << (8 * k);
+                ++cnt;
+            }
+            word[key] = wv;
+        }
+        if (j == n - 1)
+            for (uint32_t c = key + 1u; c < N; ++c) word[c] = 0u;
+    }
+    // pairs in determineCollisionType's order for 2, 3 and 4 arrivals (counts are sums, so the
+    // order only has to cover the same pairs)
+    const int npairs = cnt >= 4 ? 6 : cnt == 3 ? 3 : cnt == 2 ? 1 : 0;
+    const uint8_t PA[6] = {0, 0, 0, 1, 1, 2};
+    const uint8_t PB[6] = {1, 2, 3, 2, 3, 3};
+    const uint8_t PA3[3] = {0, 0, 1};
+    const uint8_t PB3[3] = {1, 2, 2};
+#pragma unroll
+    for (int slot = 0; slot < 6; ++slot) {
+        uint32_t keyv = 0xffffffffu;
+        uint32_t pair = 0;
+        int cat = -1;
+        if (slot < npairs) {
+            const int a = cnt == 3 ? PA3[slot] : PA[slot];
+            const int b = cnt == 3 ? PB3[slot] : PB[slot];
+            cat = evidence_category(bm, ids[a], ids[b], hs[a], hs[b], thr, cooldown, &pair);
+            if (cat >= 0) keyv = pair * 5u + (uint32_t)cat;
+        }
+        const unsigned any = __ballot_sync(0xffffffffu, keyv != 0xffffffffu);
+        if (any == 0) continue;
+        const unsigned peers = __match_any_sync(0xffffffffu, keyv);
+        if (keyv != 0xffffffffu && (peers & ((1u << lane) - 1u)) == 0)
+            atomicAdd(&counts[pair].c[cat], __popc(peers));
+    }
+}
+
+// createCollisionTypeMatrix (:890-972).  Also clears the evidence for the next step.
+__global__ void k_type_matrix(PairCounts *counts, uint8_t *bm, int cooldown, int minSize)
+{
+    const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (uint32_t)kPairs) return;
+    const PairCounts pc = counts[idx];
+    int *cp = counts[idx].c;
+    cp[0] = cp[1] = cp[2] = cp[3] = cp[4] = 0;
+    const int *c = pc.c;
+    const uint32_t packed = bm[idx];
+    const bool hasType = packed & 1u;
+    const int count = (int)((packed >> 4) & 0x0Fu);
+    const uint32_t total = (uint32_t)(c[0] + c[1] + c[2] + c[3] + c[4]);
+    if (total == 0) return;
+    if (hasType && count < cooldown) {
+        bm[idx] = (uint8_t)((packed & 0x0Fu) | (((uint32_t)(count + 1) & 0x0Fu) << 4));
+        return;
+    }
+    if (total < (uint32_t)minSize) return;
+    uint32_t out = packed & 0x0Fu;
+    const bool hasPol = (packed >> 2) & 1u;
+    const bool polA = (packed >> 3) & 1u;
+    const int oppA = c[2] + c[4], oppB = c[0] + c[4];
+    const int subA = c[0] + c[1] - oppA, subB = c[2] + c[3] - oppB;
+    if (c[4] >= c[0] + c[1] && c[4] >= c[2] + c[3]) out |= 3u;
+    else if (subA > 0 && subA > subB && (!hasPol || polA)) out = (out & ~2u) | 13u;
+    else if (subB > 0 && subB > subA && (!hasPol || !polA)) out = (out & ~10u) | 5u;
+    bm[idx] = (uint8_t)out;
+}
+
+}  // namespace
+
+int launch_plates(tecto_world *w, cudaStream_t st)
+{
+    const int rc = launch_clear_marks(w, st);  // must run before k_plates resets the list count
+    if (rc != TECTO_OK) return rc;
+    k_plates<<<1, 256, 0, st>>>(w->b.plates, w->b.off, w->b.ctl);
+    TECTO_CUDA(cudaGetLastError());
+    w->launches += 1;
+    return TECTO_OK;
+}
+
+int launch_sort_keys(tecto_world *w, cudaStream_t st)
+{
+    SortArgs a{};
+    a.gen_id = w->b.id[w->cur_id];
+    a.gen_off = w->b.off;
+    a.W = w->W;
+    a.H = w->H;
+    a.keys[0] = w->b.keys[0];
+    a.keys[1] = w->b.keys[1];
+    a.vals[0] = w->b.vals[0];
+    a.vals[1] = w->b.vals[1];
+    a.n = w->N;
+    a.key_bits = key_bits_for(w->N);
+    int half = 0;
+    const int rc = run_sort(a, w->b.sort, st, &half);
+    if (rc != TECTO_OK) return rc;
+    w->sort_final = half;
+    w->launches += 2 + (uint64_t)sort_passes_for(a.key_bits);
+    return TECTO_OK;
+}
+
+int launch_words(tecto_world *w, cudaStream_t st)
+{
+    const uint32_t n = (uint32_t)w->N;
+    const tecto_kernel_settings &ks = w->settings.kernel;
+    k_words<<<(n + 255) / 256, 256, 0, st>>>(w->b.keys[w->sort_final], w->b.vals[w->sort_final], n, n,
+                                             w->b.id[w->cur_id], w->b.h[w->cur_h], w->b.type_bitmap,
+                                             w->b.counts, w->b.word, ks.continentalCrustThreshold,
+                                             ks.collisionTypeUpdateCooldown);
+    TECTO_CUDA(cudaGetLastError());
+    w->launches += 1;
+    return TECTO_OK;
+}
+
+int launch_type_matrix(tecto_world *w, cudaStream_t st)
+{
+    const tecto_kernel_settings &ks = w->settings.kernel;
+    k_type_matrix<<<(kPairs + 255) / 256, 256, 0, st>>>(w->b.counts, w->b.type_bitmap,
+                                                        ks.collisionTypeUpdateCooldown,
+                                                        ks.minCollisionSize);
+    TECTO_CUDA(cudaGetLastError());
+    w->launches += 1;
+    return TECTO_OK;
+}
+
+}  // namespace tecto

@@ -1,0 +1,325 @@
+// k_resolve.cu - per-destination-cell resolve (divergence / movement / convergence), the
+// Gaussian uplift fused into the same tile, the divergence-bitmap flip, and accretion.
+// Reference: processCollisions and helpers, src/cuda_compute/plate_tectonics_kernel.cu:301-780.
+#include "noise.cuh"
+#include "tecto_internal.cuh"
+
+namespace tecto {
+
+namespace {
+
+constexpr int RX = 64;   // resolve tile width (cells)
+constexpr int RY = 16;   // resolve tile height
+constexpr int kMaxBlurRadius = 8;
+
+struct ResolveParams {
+    int W, H;
+    const uint32_t *word;
+    const uint8_t *id_old;
+    const float *h_old;
+    const int2 *off;
+    const uint8_t *bm;
+    const uint32_t *div_bitmap;
+    uint32_t *has_div;
+    float *h_new;
+    uint8_t *id_new;
+    unsigned long long *acc;
+    uint32_t *acc_list;
+    Control *ctl;
+    float thr;
+    float tmin, tmax, tfac;
+    float amount;
+    float wts[2 * kMaxBlurRadius + 1];
+};
+
+// determineCollisionType device function (:611-649)
+__device__ __forceinline__ uint32_t pair_type(const uint8_t *bm, uint8_t A, uint8_t B, float hA,
+                                              float hB, float thr)
+{
+    const bool cond = A < B;
+    const uint8_t mn = cond ? A : B, mx = cond ? B : A;
+    const float mnH = cond ? hA : hB, mxH = cond ? hB : hA;
+    const uint32_t packed = __ldg(bm + tri_index(mn, mx));
+    const uint32_t hasType = packed & 1u, type = (packed >> 1) & 1u, pol = (packed >> 3) & 1u;
+    uint32_t out = 0;
+    if (hasType && type == 0) {
+        if (pol == 1) out = (mnH >= thr) ? (mn == A ? 3u : 4u) : (mn == A ? 1u : 2u);
+        if (pol == 0) out = (mxH >= thr) ? (mx == A ? 3u : 4u) : (mx == A ? 1u : 2u);
+    }
+    return out;
+}
+
+__device__ __forceinline__ void mark_accretion(const ResolveParams &p, uint32_t target, uint32_t d,
+                                               uint8_t owner)
+{
+    // last writer in cell order wins (the reference writes the byte plainly, :531-555)
+    const unsigned long long v = ((unsigned long long)(d + 1u) << 8) | (unsigned long long)(255u - owner);
+    const unsigned long long old = atomicMax(p.acc + target, v);
+    if (old == 0ull) {
+        const uint32_t slot = atomicAdd(&p.ctl->acc_count, 1u);
+        p.acc_list[slot] = target;
+    }
+}
+
+// Resolve one destination cell d = (x, y); returns the new height (before uplift).
+__device__ __forceinline__ float resolve_cell(const ResolveParams &p, const int2 *s_off, int x, int y,
+                                              uint32_t d, uint32_t cv, uint32_t seed,
+                                              uint32_t iteration, uint8_t *id_out)
+{
+    const int W = p.W, H = p.H;
+    if (cv == 0u) {
+        // processDivergence (:301-362)
+        const uint8_t prev = p.id_old[d];
+        const int2 o = s_off[prev];
+        const uint32_t cvo = p.word[cidx(x - o.x, y - o.y, W, H)];
+        const uint8_t oppId = (uint8_t)((255u - cvo) & 0xFFu);
+        uint8_t nid = prev;
+        if (cvo != 0u && cvo <= 0xFFu && oppId != prev) {
+            const uint8_t mn = prev < oppId ? prev : oppId;
+            const uint8_t mx = prev < oppId ? oppId : prev;
+            const uint32_t bit = tri_index(mn, mx);
+            nid = (__ldg(p.div_bitmap + bit / 32u) & (1u << (bit % 32u))) ? mn : mx;
+            atomicOr(p.has_div + bit / 32u, 1u << (bit % 32u));
+        }
+        const float noise = simplex3((float)x, (float)y, (float)iteration, 0.01f, (int)seed);
+        const float target = p.tmin + noise * (p.tmax - p.tmin);
+        *id_out = nid;
+        return lerp_p0811(p.h_old[d], target, p.tfac);
+    }
+    uint8_t ids[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) ids[k] = (uint8_t)(255u - ((cv >> (8 * k)) & 0xFFu));
+    if (ids[1] == 255) {
+        // processMovement (:586-609)
+        const int2 o = s_off[ids[0]];
+        *id_out = ids[0];
+        return p.h_old[cidx(x - o.x, y - o.y, W, H)];
+    }
+    // processConvergence (:469-584)
+    const int n = ids[3] != 255 ? 4 : ids[2] != 255 ? 3 : 2;
+    const int pairLen = n == 4 ? 6 : n == 3 ? 3 : 1;
+    const int PA[6] = {0, 0, 1, 0, 1, 2};
+    const int PB[6] = {1, 2, 2, 3, 3, 3};
+    float heights[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    for (int k = 0; k < n; ++k) {
+        const int2 o = s_off[ids[k]];
+        heights[k] = p.h_old[cidx(x - o.x, y - o.y, W, H)];
+    }
+    uint32_t types[6];
+    bool sub[4] = {false, false, false, false};
+    for (int a = 0; a < pairLen; ++a) {
+        types[a] = pair_type(p.bm, ids[PA[a]], ids[PB[a]], heights[PA[a]], heights[PB[a]], p.thr);
+        if (types[a] == 1u || types[a] == 3u) sub[PA[a]] = true;
+        else if (types[a] == 2u || types[a] == 4u) sub[PB[a]] = true;
+    }
+    int owner = 0;
+    for (int i = 0; i < n; ++i)
+        if (!sub[i]) owner = i;
+    const uint8_t ownerId = ids[owner];
+    float writeH = heights[owner];
+    for (int a = 0; a < pairLen; ++a) {
+        const int ia = PA[a], ib = PB[a];
+        float hh;
+        if (ia == owner) hh = heights[ib];
+        else if (ib == owner) hh = heights[ia];
+        else continue;
+        if (hh > writeH) writeH = hh;  // writeHeight keeps the larger of the pair
+        int other = -1;
+        if (ia == owner && types[a] == 4u) other = ib;
+        else if (ib == owner && types[a] == 3u) other = ia;
+        if (other >= 0) {
+            const int2 oo = s_off[ids[other]];
+            uint32_t target;
+            if (oo.x != 0 || oo.y != 0) {
+                target = cidx(x - oo.x, y - oo.y, W, H);
+            } else {
+                const int2 ow = s_off[ownerId];
+                target = cidx(x + ow.x, y + ow.y, W, H);
+            }
+            mark_accretion(p, target, d, ownerId);
+        }
+    }
+    *id_out = ownerId;
+    return writeH;
+}
+
+template <int R>
+__global__ __launch_bounds__(256) void k_resolve(ResolveParams p)
+{
+    constexpr int SX = RX + 2 * R, SY = RY + 2 * R;
+    __shared__ uint32_t s_word[SY * SX];
+    __shared__ float s_tmp[(R > 0) ? SY * RX : 1];
+    __shared__ int2 s_off[kPlates + 1];
+    const int t = threadIdx.x;
+    const int x0 = blockIdx.x * RX, y0 = blockIdx.y * RY;
+    for (int i = t; i < kPlates + 1; i += 256) s_off[i] = p.off[i];
+    for (int e = t; e < SY * SX; e += 256) {
+        const int ly = e / SX, lx = e - ly * SX;
+        s_word[e] = p.word[cidx(x0 + lx - R, y0 + ly - R, p.W, p.H)];
+    }
+    __syncthreads();
+    if (R > 0) {
+        // horizontal pass of the separable blur over the convergent-cell field
+        for (int e = t; e < SY * RX; e += 256) {
+            const int ly = e / RX, lx = e - ly * RX;
+            float a = 0.0f;
+#pragma unroll
+            for (int k = -R; k <= R; ++k) {
+                const float u = s_word[ly * SX + lx + R + k] > 0xFFu ? p.amount : 0.0f;
+                a = a + p.wts[k + R] * u;
+            }
+            s_tmp[e] = a;
+        }
+        __syncthreads();
+    }
+    const uint32_t seed = p.ctl->seed, iteration = p.ctl->iteration;
+    const int lx = t % RX;
+#pragma unroll 1
+    for (int ly = t / RX; ly < RY; ly += 256 / RX) {
+        const int x = x0 + lx, y = y0 + ly;
+        if (x >= p.W || y >= p.H) continue;
+        const uint32_t d = (uint32_t)y * (uint32_t)p.W + (uint32_t)x;
+        const uint32_t cv = s_word[(ly + R) * SX + lx + R];
+        uint8_t nid;
+        float hn = resolve_cell(p, s_off, x, y, d, cv, seed, iteration, &nid);
+        if (R > 0) {
+            float a = 0.0f;
+#pragma unroll
+            for (int k = -R; k <= R; ++k) a = a + p.wts[k + R] * s_tmp[(ly + R + k) * RX + lx];
+            hn = hn + a;
+        }
+        p.h_new[d] = hn;
+        p.id_new[d] = nid;
+    }
+}
+
+// flipDivergedBitmap (:772-780); clears the per-step bits for the next step
+__global__ void k_flip(uint32_t *div_bitmap, uint32_t *has_div)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < kDivWords) {
+        div_bitmap[i] ^= has_div[i];
+        has_div[i] = 0u;
+    }
+}
+
+// applyAccretion (:747-770) over the cells that received a mark this step; clears the marks and
+// advances the step counter.
+__global__ void k_finish(unsigned long long *acc, const uint32_t *acc_list, uint8_t *acc_u8,
+                         const float *h, uint8_t *id, Control *ctl, float thr)
+{
+    const uint32_t count = ctl->acc_count;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const uint32_t c = acc_list[i];
+        const unsigned long long m = acc[c];
+        acc[c] = 0ull;
+        const uint8_t value = (uint8_t)(m & 0xFFu);
+        acc_u8[c] = value;
+        const uint8_t accId = (uint8_t)(255u - value);
+        if (accId != 255 && h[c] >= thr) id[c] = accId;
+    }
+}
+
+__global__ void k_bump_iteration(Control *ctl) { ctl->iteration += 1u; }
+
+// Clears last step's decoded marks before this step's resolve (list of the previous step).
+__global__ void k_clear_acc_u8(uint8_t *acc_u8, const uint32_t *acc_list, const Control *ctl)
+{
+    const uint32_t count = ctl->acc_count;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)
+        acc_u8[acc_list[i]] = 0;
+}
+
+}  // namespace
+
+void gaussian_weights(float sigma, int radius, float *out)
+{
+    double tmp[2 * kMaxBlurRadius + 1];
+    double sum = 0.0;
+    for (int k = -radius; k <= radius; ++k) {
+        tmp[k + radius] = exp(-(double)(k * k) / (2.0 * (double)sigma * (double)sigma));
+        sum += tmp[k + radius];
+    }
+    for (int k = 0; k <= 2 * radius; ++k) out[k] = (float)(tmp[k] / sum);
+}
+
+int launch_resolve(tecto_world *w, cudaStream_t st)
+{
+    const tecto_settings &s = w->settings;
+    ResolveParams p{};
+    p.W = w->W;
+    p.H = w->H;
+    p.word = w->b.word;
+    p.id_old = w->b.id[w->cur_id];
+    p.h_old = w->b.h[w->cur_h];
+    p.off = w->b.off;
+    p.bm = w->b.type_bitmap;
+    p.div_bitmap = w->b.div_bitmap;
+    p.has_div = w->b.has_div;
+    p.h_new = w->b.h[w->cur_h ^ 1];
+    p.id_new = w->b.id[w->cur_id ^ 1];
+    p.acc = w->b.acc;
+    p.acc_list = w->b.acc_list;
+    p.ctl = w->b.ctl;
+    p.thr = s.kernel.continentalCrustThreshold;
+    p.tmin = s.kernel.divergence_height_target_min;
+    p.tmax = s.kernel.divergence_height_target_max;
+    p.tfac = s.kernel.divergence_interpolation_factor;
+    p.amount = s.step.upliftAmount;
+    int R = 0;
+    if (s.step.upliftMode == TECTO_UPLIFT_GAUSSIAN) {
+        R = s.step.upliftRadius;
+        if (R < 0 || R > kMaxBlurRadius) {
+            set_error("upliftRadius must be in 0..8");
+            return TECTO_ERR_UNSUPPORTED;
+        }
+        gaussian_weights(s.step.upliftSigma, R, p.wts);
+    }
+    const dim3 grid((unsigned)((w->W + RX - 1) / RX), (unsigned)((w->H + RY - 1) / RY));
+    switch (R) {
+        case 0: k_resolve<0><<<grid, 256, 0, st>>>(p); break;
+        case 1: k_resolve<1><<<grid, 256, 0, st>>>(p); break;
+        case 2: k_resolve<2><<<grid, 256, 0, st>>>(p); break;
+        case 3: k_resolve<3><<<grid, 256, 0, st>>>(p); break;
+        case 4: k_resolve<4><<<grid, 256, 0, st>>>(p); break;
+        case 5: k_resolve<5><<<grid, 256, 0, st>>>(p); break;
+        case 6: k_resolve<6><<<grid, 256, 0, st>>>(p); break;
+        case 7: k_resolve<7><<<grid, 256, 0, st>>>(p); break;
+        default: k_resolve<8><<<grid, 256, 0, st>>>(p); break;
+    }
+    k_flip<<<(kDivWords + 255) / 256, 256, 0, st>>>(w->b.div_bitmap, w->b.has_div);
+    TECTO_CUDA(cudaGetLastError());
+    w->launches += 2;
+    w->cur_h ^= 1;
+    w->cur_id ^= 1;
+    return TECTO_OK;
+}
+
+int launch_finish(tecto_world *w, cudaStream_t st)
+{
+    k_finish<<<152, 256, 0, st>>>(w->b.acc, w->b.acc_list, w->b.acc_u8, w->b.h[w->cur_h],
+                                  w->b.id[w->cur_id], w->b.ctl,
+                                  w->settings.kernel.continentalCrustThreshold);
+    TECTO_CUDA(cudaGetLastError());
+    w->launches += 1;
+    return TECTO_OK;
+}
+
+// Runs before launch_plates resets the list count: clears the previous step's decoded marks.
+int launch_clear_marks(tecto_world *w, cudaStream_t st)
+{
+    k_clear_acc_u8<<<64, 256, 0, st>>>(w->b.acc_u8, w->b.acc_list, w->b.ctl);
+    TECTO_CUDA(cudaGetLastError());
+    w->launches += 1;
+    return TECTO_OK;
+}
+
+int launch_bump_iteration(tecto_world *w, cudaStream_t st)
+{
+    k_bump_iteration<<<1, 1, 0, st>>>(w->b.ctl);
+    TECTO_CUDA(cudaGetLastError());
+    w->launches += 1;
+    return TECTO_OK;
+}
+
+}  // namespace tecto

@@ -1,0 +1,370 @@
+// k_sort.cu - stable LSD radix sort of (destination cell, source cell) pairs.
+//
+// Replaces registerPlateCollisions' atomic slotting (src/cuda_compute/plate_tectonics_kernel.cu:
+// 273-298): arrivals are grouped by sorting on the destination key; the sort is stable, so
+// within one destination the sources stay in ascending order, which is the engine's canonical
+// arrival-slot order.
+//
+// Onesweep structure: one kernel builds the digit histograms of every pass in a single read;
+// then each pass is one kernel that ranks a tile of 4096 keys with warp ballots, publishes the
+// tile's digit counts, walks back over earlier tiles (decoupled look-back, bounded spin) and
+// scatters through shared memory so that runs of equal digits leave as contiguous stores.
+// The first pass can generate its keys from plate ids (advection fused into the sort: the key
+// of cell i is getPixelMovements' wrapped destination, plate_tectonics_kernel.cu:248-265).
+#include "tecto_internal.cuh"
+
+namespace tecto {
+
+namespace {
+
+constexpr int kRadix = 256;
+constexpr int kWarps = kSortThreads / 32;
+
+__device__ __forceinline__ uint32_t gen_key(size_t i, const uint8_t *id, const int2 *s_off, int W,
+                                            int H)
+{
+    const uint32_t i32 = (uint32_t)i;  // n < 2^30: 32-bit division is enough
+    const int y = (int)(i32 / (uint32_t)W);
+    const int x = (int)(i32 - (uint32_t)y * (uint32_t)W);
+    const int2 o = s_off[id[i]];
+    return cidx(x + o.x, y + o.y, W, H);
+}
+
+__device__ __forceinline__ uint32_t ld_volatile(const uint32_t *p)
+{
+    return *(const volatile uint32_t *)p;
+}
+
+__device__ __forceinline__ void st_volatile(uint32_t *p, uint32_t v)
+{
+    *(volatile uint32_t *)p = v;
+}
+
+// Digit histograms of all passes in one read of the keys.
+template <bool GEN>
+__global__ __launch_bounds__(256) void k_sort_hist(const uint8_t *gen_id, const int2 *gen_off,
+                                                   int W, int H, const uint32_t *keys_in, size_t n,
+                                                   int passes, uint32_t *hist)
+{
+    __shared__ uint32_t s_hist[kMaxSortPasses][kRadix];
+    __shared__ int2 s_off[kPlates + 1];
+    for (int i = threadIdx.x; i < kMaxSortPasses * kRadix; i += blockDim.x) (&s_hist[0][0])[i] = 0;
+    if (GEN)
+        for (int i = threadIdx.x; i < kPlates + 1; i += blockDim.x) s_off[i] = gen_off[i];
+    __syncthreads();
+    const unsigned lane = threadIdx.x & 31u;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    // every lane runs the same number of rounds so that the warp-wide match stays converged
+    const size_t rounds = (n + stride - 1) / stride;
+    for (size_t r = 0; r < rounds; ++r) {
+        const size_t i = r * stride + (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+        const bool valid = i < n;
+        uint32_t key = 0;
+        if (valid) key = GEN ? gen_key(i, gen_id, s_off, W, H) : keys_in[i];
+        for (int p = 0; p < passes; ++p) {
+            const uint32_t d = valid ? ((key >> (8 * p)) & 0xFFu) : 0x100u;
+            const unsigned peers = __match_any_sync(0xffffffffu, d);
+            if (valid && (peers & ((1u << lane) - 1u)) == 0)
+                atomicAdd(&s_hist[p][d], (uint32_t)__popc(peers));
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < passes * kRadix; i += blockDim.x) {
+        const uint32_t v = (&s_hist[0][0])[i];
+        if (v) atomicAdd(&hist[i], v);
+    }
+}
+
+// Exclusive scan of each pass's 256 digit counts, in place.  One block of 256 threads.
+__global__ void k_sort_scan(uint32_t *hist, int passes)
+{
+    __shared__ uint32_t s_w[kWarps];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    for (int p = 0; p < passes; ++p) {
+        const uint32_t v = hist[p * kRadix + t];
+        uint32_t inc = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += u;
+        }
+        if (lane == 31) s_w[warp] = inc;
+        __syncthreads();
+        uint32_t wbase = 0;
+        for (int k = 0; k < warp; ++k) wbase += s_w[k];
+        hist[p * kRadix + t] = wbase + inc - v;
+        __syncthreads();
+    }
+}
+
+// One onesweep pass.
+template <bool GEN>
+__global__ __launch_bounds__(kSortThreads) void k_sort_pass(
+    const uint8_t *gen_id, const int2 *gen_off, int W, int H, const uint32_t *keys_in,
+    const uint32_t *vals_in, uint32_t *keys_out, uint32_t *vals_out, size_t n, int shift,
+    const uint32_t *digit_start, uint32_t *status, uint32_t *tile_counter, uint32_t *error)
+{
+    __shared__ uint32_t s_cnt[kWarps][kRadix];  // per-warp digit counts, then warp offsets
+    __shared__ uint32_t s_start[kRadix];        // tile-local exclusive start per digit
+    __shared__ uint32_t s_base[kRadix];         // global output position of the digit's run
+    __shared__ uint32_t s_keys[kSortTile];
+    __shared__ uint32_t s_vals[kSortTile];
+    __shared__ int2 s_off[kPlates + 1];
+    __shared__ uint32_t s_wsum[kWarps];
+    __shared__ uint32_t s_tile;
+
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    if (t == 0) s_tile = atomicAdd(tile_counter, 1u);
+    for (int i = t; i < kWarps * kRadix; i += kSortThreads) (&s_cnt[0][0])[i] = 0;
+    if (GEN)
+        for (int i = t; i < kPlates + 1; i += kSortThreads) s_off[i] = gen_off[i];
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const size_t base = (size_t)tile * kSortTile;
+
+    uint32_t k[kSortItems], v[kSortItems], rank[kSortItems];
+    const size_t wbase = base + (size_t)warp * (32 * kSortItems);
+#pragma unroll
+    for (int it = 0; it < kSortItems; ++it) {
+        const size_t idx = wbase + (size_t)it * 32 + lane;
+        if (idx < n) {
+            if (GEN) {
+                k[it] = gen_key(idx, gen_id, s_off, W, H);
+                v[it] = (uint32_t)idx;
+            } else {
+                k[it] = keys_in[idx];
+                v[it] = vals_in[idx];
+            }
+        } else {
+            k[it] = 0;
+            v[it] = 0;
+        }
+    }
+
+    // Warp-level ranking: items are visited in element order (item, lane), so the rank of an
+    // item among equal digits of its warp preserves input order (stability).
+    const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int it = 0; it < kSortItems; ++it) {
+        const bool valid = wbase + (size_t)it * 32 + lane < n;
+        const uint32_t d = (k[it] >> shift) & 0xFFu;
+        unsigned peers = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+        for (int b = 0; b < 8; ++b) {
+            const bool bit = (d >> b) & 1u;
+            const unsigned bb = __ballot_sync(0xffffffffu, bit);
+            peers &= bit ? bb : ~bb;
+        }
+        uint32_t before = 0;
+        if (valid) before = s_cnt[warp][d];
+        __syncwarp();
+        if (valid && (peers & lt) == 0) s_cnt[warp][d] = before + (uint32_t)__popc(peers);
+        __syncwarp();
+        rank[it] = before + (uint32_t)__popc(peers & lt);
+    }
+    __syncthreads();
+
+    // Per digit (thread t owns digit t): warp offsets and the tile's count of that digit.
+    uint32_t run = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) {
+        const uint32_t c = s_cnt[w][t];
+        s_cnt[w][t] = run;
+        run += c;
+    }
+    // Exclusive scan of the tile counts over digits.
+    uint32_t inc = run;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += u;
+    }
+    if (lane == 31) s_wsum[warp] = inc;
+
+    // Decoupled look-back for digit t.
+    uint32_t *my = status + (size_t)tile * kRadix + t;
+    uint32_t prefix = 0;
+    if (tile == 0) {
+        st_volatile(my, kFlagPrefix | run);
+    } else {
+        st_volatile(my, kFlagAggregate | run);
+        int j = (int)tile - 1;
+        uint32_t spins = 0;
+        while (j >= 0) {
+            const uint32_t s = ld_volatile(status + (size_t)j * kRadix + t);
+            if ((s & ~kValueMask) == 0) {
+                if (++spins > kSpinLimit) {  // predecessor never published: flag and give up
+                    atomicOr(error, kErrLookbackTimeout);
+                    break;
+                }
+                continue;
+            }
+            prefix += s & kValueMask;
+            if (s & kFlagPrefix) break;
+            --j;
+        }
+        st_volatile(my, kFlagPrefix | ((prefix + run) & kValueMask));
+    }
+    __syncthreads();
+    uint32_t wb = 0;
+    for (int w = 0; w < warp; ++w) wb += s_wsum[w];
+    s_start[t] = wb + inc - run;
+    s_base[t] = digit_start[t] + prefix;
+    __syncthreads();
+
+    // Scatter into shared memory in digit order.
+#pragma unroll
+    for (int it = 0; it < kSortItems; ++it) {
+        if (wbase + (size_t)it * 32 + lane < n) {
+            const uint32_t d = (k[it] >> shift) & 0xFFu;
+            const uint32_t pos = s_start[d] + s_cnt[warp][d] + rank[it];
+            s_keys[pos] = k[it];
+            s_vals[pos] = v[it];
+        }
+    }
+    __syncthreads();
+    const size_t rem = n - base;
+    const uint32_t tile_n = rem < (size_t)kSortTile ? (uint32_t)rem : (uint32_t)kSortTile;
+    for (uint32_t j = t; j < tile_n; j += kSortThreads) {
+        const uint32_t key = s_keys[j];
+        const uint32_t d = (key >> shift) & 0xFFu;
+        const uint32_t out = s_base[d] + (j - s_start[d]);
+        keys_out[out] = key;
+        vals_out[out] = s_vals[j];
+    }
+}
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace
+
+int key_bits_for(size_t n)
+{
+    int b = 1;
+    while (b < 32 && ((size_t)1 << b) < n) ++b;
+    return b;
+}
+
+int sort_passes_for(int key_bits) { return (key_bits + 7) / 8; }
+
+size_t sort_scratch_bytes(size_t n, int key_bits)
+{
+    const size_t passes = (size_t)sort_passes_for(key_bits);
+    const size_t tiles = (n + kSortTile - 1) / kSortTile;
+    return align256(passes * kRadix * 4) + align256(passes * tiles * kRadix * 4) +
+           align256(kMaxSortPasses * 4) + align256(4);
+}
+
+void sort_scratch_carve(void *base, size_t n, int key_bits, SortScratch *out)
+{
+    const int passes = sort_passes_for(key_bits);
+    const size_t tiles = (n + kSortTile - 1) / kSortTile;
+    char *p = (char *)base;
+    out->passes = passes;
+    out->tiles = (int)tiles;
+    out->hist = (uint32_t *)p;
+    p += align256((size_t)passes * kRadix * 4);
+    out->status = (uint32_t *)p;
+    p += align256((size_t)passes * tiles * kRadix * 4);
+    out->counters = (uint32_t *)p;
+    p += align256(kMaxSortPasses * 4);
+    out->error = (uint32_t *)p;
+}
+
+int run_sort(const SortArgs &a, const SortScratch &scr, cudaStream_t st, int *result_half)
+{
+    const int passes = sort_passes_for(a.key_bits);
+    if (passes != scr.passes || a.n == 0 || a.n > (size_t)kValueMask) {
+        set_error("run_sort: scratch does not match the problem size");
+        return TECTO_ERR_INVALID;
+    }
+    const size_t tiles = (a.n + kSortTile - 1) / kSortTile;
+    // one memset covers hist, status and counters (contiguous in the scratch layout)
+    const size_t clear = align256((size_t)passes * kRadix * 4) +
+                         align256((size_t)passes * tiles * kRadix * 4) + align256(kMaxSortPasses * 4);
+    TECTO_CUDA(cudaMemsetAsync(scr.hist, 0, clear, st));
+    const bool gen = a.gen_id != nullptr;
+    int hist_blocks = (int)((a.n + 255) / 256);
+    if (hist_blocks > 152 * 8) hist_blocks = 152 * 8;
+    if (gen)
+        k_sort_hist<true><<<hist_blocks, 256, 0, st>>>(a.gen_id, a.gen_off, a.W, a.H, nullptr, a.n,
+                                                        passes, scr.hist);
+    else
+        k_sort_hist<false><<<hist_blocks, 256, 0, st>>>(nullptr, nullptr, a.W, a.H, a.keys_in, a.n,
+                                                         passes, scr.hist);
+    k_sort_scan<<<1, kRadix, 0, st>>>(scr.hist, passes);
+    int half = 0;
+    const uint32_t *kin = a.keys_in, *vin = a.vals_in;
+    for (int p = 0; p < passes; ++p) {
+        uint32_t *kout = a.keys[half], *vout = a.vals[half];
+        uint32_t *status = scr.status + (size_t)p * tiles * kRadix;
+        if (p == 0 && gen)
+            k_sort_pass<true><<<(unsigned)tiles, kSortThreads, 0, st>>>(
+                a.gen_id, a.gen_off, a.W, a.H, nullptr, nullptr, kout, vout, a.n, 0, scr.hist,
+                status, scr.counters + p, scr.error);
+        else
+            k_sort_pass<false><<<(unsigned)tiles, kSortThreads, 0, st>>>(
+                nullptr, nullptr, a.W, a.H, kin, vin, kout, vout, a.n, 8 * p,
+                scr.hist + p * kRadix, status, scr.counters + p, scr.error);
+        kin = kout;
+        vin = vout;
+        half ^= 1;
+    }
+    TECTO_CUDA(cudaGetLastError());
+    *result_half = half ^ 1;
+    return TECTO_OK;
+}
+
+}  // namespace tecto
+
+// ---- C ABI: standalone sort -------------------------------------------------------------------
+
+extern "C" size_t tecto_sort_scratch_bytes(size_t n, int key_bits)
+{
+    if (key_bits < 1 || key_bits > 32) return 0;
+    // two ping-pong halves for keys and values are carved after the sort's own scratch
+    return tecto::sort_scratch_bytes(n, key_bits) + 4 * tecto::align256(n * sizeof(uint32_t));
+}
+
+extern "C" int tecto_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_out,
+                                uint32_t *vals_out, size_t n, int key_bits, void *scratch,
+                                size_t scratch_bytes, tecto_stream_t stream)
+{
+    using namespace tecto;
+    if (n == 0) return TECTO_OK;
+    if (!keys_in || !vals_in || !keys_out || !vals_out || !scratch || key_bits < 1 ||
+        key_bits > 32 || n > (size_t)kValueMask) {
+        set_error("tecto_sort_pairs: invalid argument");
+        return TECTO_ERR_INVALID;
+    }
+    if (scratch_bytes < tecto_sort_scratch_bytes(n, key_bits)) {
+        set_error("tecto_sort_pairs: scratch too small");
+        return TECTO_ERR_INVALID;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    SortScratch scr{};
+    sort_scratch_carve(scratch, n, key_bits, &scr);
+    char *p = (char *)scratch + sort_scratch_bytes(n, key_bits);
+    const size_t arr = align256(n * sizeof(uint32_t));
+    SortArgs a{};
+    a.keys_in = keys_in;
+    a.vals_in = vals_in;
+    a.keys[0] = (uint32_t *)p;
+    a.vals[0] = (uint32_t *)(p + arr);
+    a.keys[1] = (uint32_t *)(p + 2 * arr);
+    a.vals[1] = (uint32_t *)(p + 3 * arr);
+    a.n = n;
+    a.key_bits = key_bits;
+    TECTO_CUDA(cudaMemsetAsync(scr.error, 0, 4, st));
+    int half = 0;
+    const int rc = run_sort(a, scr, st, &half);
+    if (rc != TECTO_OK) return rc;
+    TECTO_CUDA(cudaMemcpyAsync(keys_out, a.keys[half], n * 4, cudaMemcpyDeviceToDevice, st));
+    TECTO_CUDA(cudaMemcpyAsync(vals_out, a.vals[half], n * 4, cudaMemcpyDeviceToDevice, st));
+    uint32_t err = 0;
+    TECTO_CUDA(cudaMemcpyAsync(&err, scr.error, 4, cudaMemcpyDeviceToHost, st));
+    TECTO_CUDA(cudaStreamSynchronize(st));
+    if (err) {
+        set_error("tecto_sort_pairs: look-back wait gave up");
+        return TECTO_ERR_DEVICE_TIMEOUT;
+    }
+    return TECTO_OK;
+}

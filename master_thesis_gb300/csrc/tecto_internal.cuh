@@ -1,0 +1,175 @@
+// tecto_internal.cuh - world layout in HBM, launch parameters and device helpers shared by the
+// engine's kernels.  Reference paths are relative to MarWo22/master_thesis.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+#include <string>
+
+#include "../../include/tecto.h"
+#include "../../include/tecto_math.h"
+
+namespace tecto {
+
+constexpr int kPlates = TECTO_MAX_PLATES;       // plate ids 0..254; byte 0 in a word = no plate
+constexpr int kPairs = TECTO_NUM_PAIRS;
+constexpr int kDivWords = TECTO_NUM_DIV_WORDS;
+constexpr int kSortTile = 4096;                 // keys per onesweep tile (256 threads x 16)
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = kSortTile / kSortThreads;
+constexpr int kMaxSortPasses = 4;               // 32-bit keys, 8-bit digits
+
+// Status word of the decoupled look-back: 2 flag bits + 30 value bits.
+constexpr uint32_t kFlagAggregate = 1u << 30;
+constexpr uint32_t kFlagPrefix = 2u << 30;
+constexpr uint32_t kValueMask = (1u << 30) - 1u;
+constexpr uint32_t kSpinLimit = 1u << 24;       // bounded waits: give up, flag, carry on
+
+// Device error flag bits (control block).
+constexpr uint32_t kErrLookbackTimeout = 1u;
+
+// Per-pair collision evidence, CollisionTypeCounts field order
+// (src/cuda_compute/plate_tectonics_kernel.cuh:47-54).
+struct PairCounts {
+    int c[5];  // subductionsAContinental, subductionsAOceanic, subductionsBContinental,
+               // subductionsBOceanic, continental
+};
+
+// Small device-resident control block; kernels read the step counter from here so that a
+// captured graph replays correctly step after step.
+struct Control {
+    uint32_t iteration;     // PlateTectonicSim::m_iterations
+    uint32_t seed;          // PlateTectonicSim::m_seed
+    uint32_t error;         // kErr* bits
+    uint32_t acc_count;     // entries in the accretion target list this step
+    uint32_t tile_counter[kMaxSortPasses];  // onesweep dynamic tile ids, one per pass
+    uint32_t pad[8];
+};
+
+// Scratch of the radix sort (histograms, look-back status).  Sizes in tecto_sort_scratch_bytes.
+struct SortScratch {
+    uint32_t *hist;      // [passes][256] digit counts -> exclusive digit starts
+    uint32_t *status;    // [passes][tiles][256] look-back words
+    uint32_t *counters;  // [passes] dynamic tile counters
+    uint32_t *error;     // error flag word
+    int passes;
+    int tiles;
+};
+
+// Device buffers of one world.  Structure of arrays, one cudaMalloc'd arena.
+struct WorldBuffers {
+    float *h[2];            // height, ping-pong
+    float *w[2];            // water
+    float *s[2];            // sediment
+    float4 *flux[2];        // outflow flux (left, +y, right, -y)
+    uint8_t *id[2];         // plate ids
+    uint32_t *word;         // packed arrivals per destination cell
+    uint32_t *keys[2];      // sort ping-pong
+    uint32_t *vals[2];
+    uint32_t *labels;       // CCL labels
+    float2 *vel;            // water velocity, split hydraulic path only
+    float *s1;              // sediment before transport, split hydraulic path only
+    unsigned long long *acc;  // accretion marks: ((dest + 1) << 8) | (255 - owner), atomicMax
+    uint32_t *acc_list;     // cells with a mark this step
+    uint8_t *acc_u8;        // decoded marks of the last step (download only)
+    uint8_t *type_bitmap;   // [kPairs]
+    uint32_t *div_bitmap;   // [kDivWords]
+    uint32_t *has_div;      // [kDivWords]
+    PairCounts *counts;     // [kPairs]
+    tecto_plate *plates;    // [kPlates]
+    int2 *off;              // [kPlates + 1] this step's integer displacement per plate
+    Control *ctl;
+    SortScratch sort;
+};
+
+}  // namespace tecto
+
+struct tecto_world {
+    int W = 0, H = 0;
+    size_t N = 0;
+    int device = 0;
+    tecto_settings settings{};
+    uint32_t seed = 0;
+    uint32_t iteration = 0;        // host mirror of ctl->iteration
+    int cur_h = 0, cur_wsf = 0, cur_id = 0;  // which ping-pong half holds the state
+    int sort_final = 0;            // which keys/vals half holds the last sorted result
+    uint64_t launches = 0;         // kernels enqueued (graph replays count their captured kernels)
+    void *arena = nullptr;
+    size_t arena_bytes = 0;
+    tecto::WorldBuffers b{};
+    // CUDA graphs of one step, keyed by (cur_h, cur_wsf, cur_id, ccl)
+    cudaGraphExec_t graphs[16] = {};
+    bool graph_valid[16] = {};
+    int graph_end[16][4] = {};     // cur_h, cur_wsf, cur_id, sort_final after the graph's step
+    uint64_t graph_launches[16] = {};
+};
+
+namespace tecto {
+
+// Thread-local last error text for tecto_last_error_string.
+void set_error(const std::string &msg);
+int cuda_fail(cudaError_t e, const char *what);
+
+#define TECTO_CUDA(call)                                          \
+    do {                                                          \
+        cudaError_t e_ = (call);                                  \
+        if (e_ != cudaSuccess) return ::tecto::cuda_fail(e_, #call); \
+    } while (0)
+
+// ---- device helpers ---------------------------------------------------------------------
+
+// CudaTexture::wrapCoordinate (src/cuda_compute/types/cuda_texture.cuh:67-76)
+__host__ __device__ __forceinline__ int wrapc(int c, int n)
+{
+    const int r = c % n;
+    return r + (n & (r >> 31));
+}
+
+__host__ __device__ __forceinline__ uint32_t cidx(int x, int y, int W, int H)
+{
+    return (uint32_t)(wrapc(y, H) * W + wrapc(x, W));
+}
+
+// upperTriangleIndexUnchecked(i, j, 255), i < j (src/cuda_compute/cuda_helper.cuh:97-104)
+__host__ __device__ __forceinline__ uint32_t tri_index(uint32_t i, uint32_t j)
+{
+    return i * (2u * kPlates - i - 1u) / 2u + (j - i - 1u);
+}
+
+// ---- phase launchers (each enqueues on `st`) ----------------------------------------------
+int launch_plates(tecto_world *w, cudaStream_t st);
+int launch_sort_keys(tecto_world *w, cudaStream_t st);
+int launch_words(tecto_world *w, cudaStream_t st);
+int launch_type_matrix(tecto_world *w, cudaStream_t st);
+int launch_resolve(tecto_world *w, cudaStream_t st);
+int launch_thermal(tecto_world *w, int iterations, cudaStream_t st);
+int launch_hydraulic(tecto_world *w, int iterations, float dt, cudaStream_t st);
+int launch_finish(tecto_world *w, cudaStream_t st);
+int launch_clear_marks(tecto_world *w, cudaStream_t st);
+int launch_bump_iteration(tecto_world *w, cudaStream_t st);
+void gaussian_weights(float sigma, int radius, float *out);
+int launch_ccl(tecto_world *w, int connectivity, cudaStream_t st);
+
+// Radix sort core (k_sort.cu).  If gen_id != nullptr the first pass generates keys (destination
+// cells) and values (source cells) from plate ids and the per-plate displacement `off`;
+// otherwise it reads keys_in/vals_in.  Returns the half (0/1) of keys/vals holding the result.
+struct SortArgs {
+    const uint8_t *gen_id;
+    const int2 *gen_off;
+    int W, H;
+    const uint32_t *keys_in;
+    const uint32_t *vals_in;
+    uint32_t *keys[2];
+    uint32_t *vals[2];
+    size_t n;
+    int key_bits;
+};
+int sort_passes_for(int key_bits);
+size_t sort_scratch_bytes(size_t n, int key_bits);
+void sort_scratch_carve(void *base, size_t n, int key_bits, SortScratch *out);
+int run_sort(const SortArgs &a, const SortScratch &scr, cudaStream_t st, int *result_half);
+
+int key_bits_for(size_t n);
+
+}  // namespace tecto

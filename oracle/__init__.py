@@ -1,0 +1,186 @@
+"""Python access to the CPU oracle (oracle/_build/liboracle.so) and, where it has been built here,
+to the reference's own kernels compiled for the CPU (oracle/_ref/libtecto_ref.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline leg; never by the engine.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "liboracle.so"
+REF_LIB = HERE / "_ref" / "libtecto_ref.so"
+
+_o = None
+_r = None
+
+
+def build(ref: bool = False) -> None:
+    """make the oracle (and, with ref=True, the reference-on-CPU library)."""
+    targets = ["all"] + (["ref"] if ref else [])
+    subprocess.run(["make", "-s", "-C", str(HERE), *targets], check=True)
+
+
+def _P(a):
+    return a.ctypes.data if a is not None else None
+
+
+def lib() -> C.CDLL:
+    global _o
+    if _o is None:
+        if not LIB.exists():
+            build()
+        L = C.CDLL(str(LIB))
+        V = C.c_void_p
+        L.or_plate_offsets.argtypes = [V, V, V, V]
+        L.or_collision_words.argtypes = [C.c_int, C.c_int, V, V, V, V, V, V, V]
+        L.or_collision_types.argtypes = [C.c_int, C.c_int, V, V, V, V, V, V]
+        L.or_resolve.argtypes = [C.c_int, C.c_int, V, V, V, V, V, V, V, V, C.c_uint32, C.c_uint32, V, V, V]
+        L.or_thermal.argtypes = [C.c_int, C.c_int, V, C.c_int, V]
+        L.or_hydraulic.argtypes = [C.c_int, C.c_int, V, V, V, V, C.c_int, C.c_float, C.c_uint32, V]
+        L.or_accretion.argtypes = [C.c_int, C.c_int, V, V, V, V]
+        L.or_ccl.argtypes = [C.c_int, C.c_int, V, V, C.c_int]
+        L.or_step.argtypes = [C.c_int, C.c_int, V, V, V, V, V, V, V, V, V, V, V, V, C.c_uint32, V]
+        L.or_hash.argtypes = [C.c_uint32]
+        L.or_hash.restype = C.c_uint32
+        L.or_simplex3.argtypes = [C.c_float] * 4 + [C.c_int]
+        L.or_simplex3.restype = C.c_float
+        L.or_rain_noise.argtypes = [C.c_int, C.c_int, C.c_int]
+        L.or_rain_noise.restype = C.c_float
+        L.or_lerp.argtypes = [C.c_float] * 3
+        L.or_lerp.restype = C.c_float
+        L.or_sinf.argtypes = [C.c_float]
+        L.or_sinf.restype = C.c_float
+        L.or_gaussian_weights.argtypes = [C.c_float, C.c_int, V]
+        L.or_use_libm_sin.argtypes = [C.c_int]
+        _o = L
+    return _o
+
+
+def use_libm_sin(on: bool) -> None:
+    """Pinning mode: the oracle calls libm's sinf, as the reference's kernels do on the CPU."""
+    lib().or_use_libm_sin(1 if on else 0)
+
+
+def ref_available() -> bool:
+    return REF_LIB.exists()
+
+
+def ref() -> C.CDLL:
+    """The reference's own kernels compiled for the CPU (only where oracle/Makefile `ref` ran)."""
+    global _r
+    if _r is None:
+        L = C.CDLL(str(REF_LIB))
+        V = C.c_void_p
+        L.ref_set_settings.argtypes = [V]
+        L.ref_pixel_movements.argtypes = [C.c_int, C.c_int, V, V, V]
+        L.ref_register_collisions.argtypes = [C.c_int, C.c_int, V, V, V]
+        L.ref_collision_types.argtypes = [C.c_int, C.c_int, V, V, V, V, V]
+        L.ref_process_collisions.argtypes = [C.c_int, C.c_int, V, V, V, V, V, V, C.c_int, C.c_uint, V, V, V, V, V]
+        L.ref_thermal.argtypes = [C.c_int, C.c_int, V]
+        L.ref_hydraulic.argtypes = [C.c_int, C.c_int, V, V, V, V, C.c_int, C.c_float, C.c_uint]
+        L.ref_hydraulic.restype = C.c_int
+        L.ref_accretion.argtypes = [C.c_int, C.c_int, V, V, V]
+        L.ref_ccl.argtypes = [C.c_int, C.c_int, V, V]
+        _r = L
+    return _r
+
+
+# ---- oracle phases on numpy arrays ---------------------------------------------------------
+
+def plate_offsets(plates: np.ndarray):
+    offx = np.zeros(255, np.int32)
+    offy = np.zeros(255, np.int32)
+    nxt = np.zeros_like(plates)
+    lib().or_plate_offsets(_P(plates), _P(offx), _P(offy), _P(nxt))
+    return offx, offy, nxt
+
+
+def collision_words(ids: np.ndarray, offx, offy):
+    H, W = ids.shape
+    N = W * H
+    dest = np.zeros(N, np.uint32)
+    word = np.zeros(N, np.uint32)
+    sk = np.zeros(N, np.uint32)
+    sv = np.zeros(N, np.uint32)
+    lib().or_collision_words(W, H, _P(ids), _P(offx), _P(offy), _P(dest), _P(word), _P(sk), _P(sv))
+    return dest.reshape(H, W), word.reshape(H, W), sk, sv
+
+
+def collision_types(word, h_old, offx, offy, settings, bitmap):
+    H, W = word.shape
+    bm = bitmap.copy()
+    lib().or_collision_types(W, H, _P(word), _P(h_old), _P(offx), _P(offy), C.addressof(settings.kernel), _P(bm))
+    return bm
+
+
+def resolve(id_old, h_old, word, offx, offy, bitmap, div_bitmap, settings, seed, iteration):
+    H, W = id_old.shape
+    div = div_bitmap.copy()
+    h_new = np.zeros_like(h_old)
+    id_new = np.zeros_like(id_old)
+    acc = np.zeros_like(id_old)
+    lib().or_resolve(W, H, _P(id_old), _P(h_old), _P(word), _P(offx), _P(offy), _P(bitmap), _P(div),
+                     C.addressof(settings), seed, iteration, _P(h_new), _P(id_new), _P(acc))
+    return h_new, id_new, acc, div
+
+
+def thermal(h, iters, settings):
+    H, W = h.shape
+    out = h.copy()
+    lib().or_thermal(W, H, _P(out), iters, C.addressof(settings.kernel))
+    return out
+
+
+def hydraulic(h, w, s, flux, iters, dt, rain_seed, settings):
+    H, W = h.shape
+    h, w, s, flux = h.copy(), w.copy(), s.copy(), flux.copy()
+    lib().or_hydraulic(W, H, _P(h), _P(w), _P(s), _P(flux), iters, dt, rain_seed, C.addressof(settings.kernel))
+    return h, w, s, flux
+
+
+def accretion(h, acc, ids, settings):
+    H, W = h.shape
+    out = ids.copy()
+    lib().or_accretion(W, H, _P(h), _P(acc), _P(out), C.addressof(settings.kernel))
+    return out
+
+
+def ccl(ids, mode):
+    H, W = ids.shape
+    labels = np.zeros((H, W), np.uint32)
+    lib().or_ccl(W, H, _P(ids), _P(labels), mode)
+    return labels
+
+
+class OracleWorld:
+    """A full world state stepped by or_step."""
+
+    def __init__(self, settings, h, ids, plates, seed, w=None, s=None, flux=None):
+        H, W = h.shape
+        self.W, self.H = W, H
+        self.settings = settings
+        self.h = h.astype(np.float32).copy()
+        self.id = ids.astype(np.uint8).copy()
+        self.w = np.zeros((H, W), np.float32) if w is None else w.copy()
+        self.s = np.zeros((H, W), np.float32) if s is None else s.copy()
+        self.flux = np.zeros((H, W, 4), np.float32) if flux is None else flux.copy()
+        self.labels = np.zeros((H, W), np.uint32)
+        self.word = np.zeros((H, W), np.uint32)
+        self.acc = np.zeros((H, W), np.uint8)
+        self.bitmap = np.zeros(32385, np.uint8)
+        self.div = np.zeros(1013, np.uint32)
+        self.plates = plates.copy()
+        self.seed = seed
+        self.iteration = C.c_uint32(0)
+
+    def step(self, n: int = 1) -> None:
+        for _ in range(n):
+            lib().or_step(self.W, self.H, _P(self.h), _P(self.w), _P(self.s), _P(self.flux), _P(self.id),
+                          _P(self.labels), _P(self.word), _P(self.acc), _P(self.bitmap), _P(self.div),
+                          _P(self.plates), C.addressof(self.settings), self.seed, C.byref(self.iteration))

@@ -1,0 +1,216 @@
+/*
+ * ref_harness.cpp - runs the reference's own hot-path kernels (MarWo22/master_thesis,
+ * src/cuda_compute/, compiled for the CPU through refshim/shim.h by oracle/Makefile) on host
+ * arrays.  TEST INFRASTRUCTURE ONLY: it produces the golden vectors under tests/golden/ that pin
+ * the C oracle.  Each kernel launch is emulated sequentially, threads in ascending global index.
+ *
+ * Launch shapes follow the reference: pixel kernels over W*H threads in blocks of 256
+ * (plate_tectonic_sim.h:15); the six unguarded hydraulic kernels need W*H % 256 == 0, which the
+ * entry points check.
+ */
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "plate_tectonics_kernel.cuh"
+#include "ccl.cuh"
+#include "kernel_settings.cuh"
+#include "plate_tectonic_sim.h"
+#include "../include/tecto.h"
+
+thread_local uint3 threadIdx;
+thread_local uint3 blockIdx;
+thread_local dim3 blockDim;
+thread_local dim3 gridDim;
+/* storage behind the one dynamically sized shared array in the kernel file (findPlausibleSplitLine,
+ * plate_tectonics_kernel.cu:2242, off the hot path and never launched here) */
+float w_l_buffer[1];
+
+static_assert(sizeof(KernelSettings) == sizeof(tecto_kernel_settings),
+              "tecto_kernel_settings must mirror KernelSettings");
+
+namespace {
+
+constexpr unsigned TPB = 256;
+
+template <class F>
+void launch(unsigned blocks, unsigned threads, F &&f)
+{
+    gridDim.x = blocks;
+    blockDim.x = threads;
+    for (unsigned b = 0; b < blocks; ++b)
+        for (unsigned t = 0; t < threads; ++t) {
+            blockIdx.x = b;
+            threadIdx.x = t;
+            f();
+        }
+}
+
+unsigned blocks_for(size_t n) { return (unsigned)((n + TPB - 1) / TPB); }
+
+std::vector<PlateData> make_plates(const tecto_plate *p)
+{
+    std::vector<PlateData> out(MAX_PLATE_COUNT);
+    for (unsigned k = 0; k < MAX_PLATE_COUNT; ++k) {
+        out[k].velocity = p[k].velocity;
+        out[k].direction = Vec2<float>(p[k].direction_x, p[k].direction_y);
+        out[k].pixelCenter = Vec2<float>(p[k].pixelCenter_x, p[k].pixelCenter_y);
+        out[k].mass = 1.0f;
+    }
+    return out;
+}
+
+} // namespace
+
+extern "C" {
+
+void ref_set_settings(const tecto_kernel_settings *ks)
+{
+    std::memcpy(&kernelSettingsHost, ks, sizeof(KernelSettings));
+    copyHostKernelSettingsToDevice();
+}
+
+/* getPixelMovements (plate_tectonics_kernel.cu:232-271) */
+void ref_pixel_movements(int W, int H, const uint8_t *id, const tecto_plate *plates, uint32_t *dest)
+{
+    std::vector<uint8_t> idc(id, id + (size_t)W * H), idcopy((size_t)W * H);
+    auto pd = make_plates(plates);
+    CudaTexture<uint8_t> tId(idc.data(), Vec2<int>(W, H)), tIdOut(idcopy.data(), Vec2<int>(W, H));
+    CudaTexture<unsigned int> tDest(dest, Vec2<int>(W, H));
+    launch(blocks_for((size_t)W * H), TPB,
+           [&] { getPixelMovements(&tId, pd.data(), &tDest, &tIdOut); });
+}
+
+/* registerPlateCollisions (plate_tectonics_kernel.cu:273-298) */
+void ref_register_collisions(int W, int H, const uint8_t *id, const uint32_t *dest, uint32_t *word)
+{
+    const size_t N = (size_t)W * H;
+    std::vector<uint8_t> idc(id, id + N);
+    std::vector<unsigned int> destc(dest, dest + N);
+    std::vector<int> counts(N, 0);
+    std::memset(word, 0, N * sizeof(uint32_t));
+    CudaTexture<uint8_t> tId(idc.data(), Vec2<int>(W, H));
+    CudaTexture<unsigned int> tDest(destc.data(), Vec2<int>(W, H));
+    CudaTexture<int> tCnt(counts.data(), Vec2<int>(W, H));
+    CudaTexture<uint32_t> tWord(word, Vec2<int>(W, H));
+    launch(blocks_for(N), TPB, [&] { registerPlateCollisions(&tId, &tDest, &tCnt, &tWord); });
+}
+
+/* determineCollisionType kernel + createCollisionTypeMatrix (plate_tectonic_sim.cu:232-241) */
+void ref_collision_types(int W, int H, const uint8_t *id_old, const float *h_old, const uint32_t *word,
+                         const tecto_plate *plates, uint8_t *type_bitmap)
+{
+    const size_t N = (size_t)W * H;
+    std::vector<uint8_t> idc(id_old, id_old + N);
+    std::vector<float> hc(h_old, h_old + N);
+    std::vector<uint32_t> wc(word, word + N);
+    auto pd = make_plates(plates);
+    std::vector<CollisionTypeCounts> counts(MAX_PLATE_COUNT * MAX_PLATE_COUNT);
+    std::memset(counts.data(), 0, counts.size() * sizeof(CollisionTypeCounts));
+    CudaTexture<uint8_t> tId(idc.data(), Vec2<int>(W, H));
+    CudaTexture<float> tH(hc.data(), Vec2<int>(W, H));
+    CudaTexture<uint32_t> tWord(wc.data(), Vec2<int>(W, H));
+    const PlateTexturesRead rd = {&tId, &tH, pd.data()};
+    launch(blocks_for(N), TPB, [&] { determineCollisionType(rd, &tWord, type_bitmap, counts.data()); });
+    launch(NUM_BLOCKS_TRIANGLE_ENTRIES, TPB,
+           [&] { createCollisionTypeMatrix(counts.data(), type_bitmap); });
+}
+
+/* processCollisions + flipDivergedBitmap (plate_tectonic_sim.cu:246-262) */
+void ref_process_collisions(int W, int H, const uint8_t *id_old, const float *h_old,
+                            const uint32_t *word, const tecto_plate *plates,
+                            const uint8_t *type_bitmap, uint32_t *div_bitmap, int seed,
+                            unsigned iteration, float *h_new, uint8_t *id_new, uint8_t *acc,
+                            float *uplift_height, uint8_t *uplift_types)
+{
+    const size_t N = (size_t)W * H;
+    std::vector<uint8_t> idc(id_old, id_old + N);
+    std::vector<float> hc(h_old, h_old + N);
+    std::vector<uint32_t> wc(word, word + N);
+    std::vector<uint8_t> bm(type_bitmap, type_bitmap + NUM_TRIANGLE_ENTRIES);
+    auto pd = make_plates(plates);
+    std::vector<uint32_t> hasDiv(NUM_WORDS_TRIANGLE_SINGLE_BITS, 0);
+    std::vector<UpliftData> up(N);
+    std::vector<CollisionVelocityChanges> vchg(MAX_PLATE_COUNT);
+    std::memset(acc, 0, N);
+    CudaTexture<uint8_t> tId(idc.data(), Vec2<int>(W, H)), tIdNew(id_new, Vec2<int>(W, H)),
+        tAcc(acc, Vec2<int>(W, H));
+    CudaTexture<float> tH(hc.data(), Vec2<int>(W, H)), tHNew(h_new, Vec2<int>(W, H));
+    CudaTexture<uint32_t> tWord(wc.data(), Vec2<int>(W, H));
+    CudaTexture<UpliftData> tUp(up.data(), Vec2<int>(W, H));
+    const PlateTexturesRead rd = {&tId, &tH, pd.data()};
+    const PlateTexturesWrite wr = {&tIdNew, &tHNew};
+    const NoiseParameters np = {seed, iteration};
+    launch(blocks_for(N), TPB, [&] {
+        processCollisions(rd, &tWord, div_bitmap, bm.data(), wr, hasDiv.data(), &tUp, &tAcc,
+                          vchg.data(), np);
+    });
+    launch(NUM_BLOCKS_TRIANGLE_SINGLE_BITS, TPB,
+           [&] { flipDivergedBitmap(div_bitmap, hasDiv.data()); });
+    for (size_t i = 0; i < N; ++i) {
+        if (uplift_height) uplift_height[i] = up[i].cumulativeHeight;
+        if (uplift_types) uplift_types[i] = up[i].collisionTypes;
+    }
+}
+
+/* thermalErosionKernel (plate_tectonics_kernel.cu:2735-2786), one launch, in place */
+void ref_thermal(int W, int H, float *h)
+{
+    CudaTexture<float> tH(h, Vec2<int>(W, H));
+    launch(blocks_for((size_t)W * H), TPB, [&] { thermalErosionKernel(&tH); });
+}
+
+/* applyHydraulicErosion's loop body (plate_tectonic_sim.cu:336-371), `iters` times */
+int ref_hydraulic(int W, int H, float *h, float *w, float *s, float *flux, int iters, float dt,
+                  unsigned rain_seed)
+{
+    const size_t N = (size_t)W * H;
+    if (N % TPB != 0) return -1;
+    std::vector<float4> f(N), fbuf(N);
+    std::memcpy(f.data(), flux, N * sizeof(float4));
+    std::vector<float> hcopy(N), sbuf(N);
+    std::vector<Vec2<float>> vel(N);
+    CudaTexture<float> tH(h, Vec2<int>(W, H)), tW(w, Vec2<int>(W, H)), tS(s, Vec2<int>(W, H)),
+        tHc(hcopy.data(), Vec2<int>(W, H)), tSb(sbuf.data(), Vec2<int>(W, H));
+    CudaTexture<float4> tF(f.data(), Vec2<int>(W, H)), tFb(fbuf.data(), Vec2<int>(W, H));
+    CudaTexture<Vec2<float>> tV(vel.data(), Vec2<int>(W, H));
+    const unsigned nb = (unsigned)(N / TPB);
+    for (int i = 0; i < iters; ++i) {
+        launch(nb, TPB, [&] { rain(&tW, dt, rain_seed); });
+        launch(nb, TPB, [&] { ::flux(&tH, &tW, &tF, &tFb, dt); });
+        launch(nb, TPB, [&] { flow(&tW, &tFb, &tF, &tV, dt); });
+        std::memcpy(hcopy.data(), h, N * sizeof(float));
+        launch(nb, TPB, [&] { sediment(&tHc, &tH, &tS, &tV, dt); });
+        launch(nb, TPB, [&] { transport(&tS, &tSb, &tV, dt); });
+        launch(nb, TPB, [&] { evaporate(&tW, dt); });
+        std::memcpy(s, sbuf.data(), N * sizeof(float));
+    }
+    std::memcpy(flux, f.data(), N * sizeof(float4));
+    return 0;
+}
+
+/* applyAccretion (plate_tectonics_kernel.cu:747-770), in place on id */
+void ref_accretion(int W, int H, const float *h, const uint8_t *acc, uint8_t *id)
+{
+    const size_t N = (size_t)W * H;
+    std::vector<float> hc(h, h + N);
+    std::vector<uint8_t> ac(acc, acc + N);
+    CudaTexture<float> tH(hc.data(), Vec2<int>(W, H));
+    CudaTexture<uint8_t> tAcc(ac.data(), Vec2<int>(W, H)), tId(id, Vec2<int>(W, H));
+    launch(blocks_for(N), TPB, [&] { applyAccretion(&tH, &tAcc, &tId); });
+}
+
+/* applyCCL's labelling kernels (plate_tectonic_sim.cu:380-389, ccl.cu:90-177) */
+void ref_ccl(int W, int H, const uint8_t *id, uint32_t *labels)
+{
+    const size_t N = (size_t)W * H;
+    std::vector<uint8_t> idc(id, id + N);
+    CudaTexture<uint8_t> tId(idc.data(), Vec2<int>(W, H));
+    CudaTexture<unsigned int> tL(labels, Vec2<int>(W, H));
+    launch(blocks_for(N), TPB, [&] { init(&tId, &tL); });
+    launch(blocks_for(N), TPB, [&] { analyzeClamped(&tL); });
+    launch(blocks_for(N), TPB, [&] { reduce(&tId, &tL); });
+    launch(blocks_for(N), TPB, [&] { analyzeUnclamped(&tL); });
+}
+
+} // extern "C"

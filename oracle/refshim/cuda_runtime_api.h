@@ -1,0 +1,2 @@
+/* shim: see shim.h */
+#include "shim.h"

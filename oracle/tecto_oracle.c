@@ -1,0 +1,742 @@
+/*
+ * tecto_oracle.c - CPU oracle for the plate-tectonics step.  TEST INFRASTRUCTURE ONLY.
+ * See tecto_oracle.h for the contract.  Reference paths are relative to MarWo22/master_thesis.
+ *
+ * Build: gcc -O2 -fopenmp -ffp-contract=off -fPIC -shared (oracle/Makefile).
+ */
+#include "tecto_oracle.h"
+#include "../include/tecto_math.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define NPLATE 255u
+
+/* ---- addressing --------------------------------------------------------------------- */
+
+/* CudaTexture::wrapCoordinate (src/cuda_compute/types/cuda_texture.cuh:67-76) */
+static inline int wrapc(int c, int n)
+{
+    const int r = c % n;
+    return r + (n & (r >> 31));
+}
+
+/* CudaTexture::coordinateToIndex (cuda_texture.cuh:55-60): wrapped y * W + x */
+static inline uint32_t cidx(int x, int y, int W, int H)
+{
+    return (uint32_t)(wrapc(y, H) * W + wrapc(x, W));
+}
+
+/* upperTriangleIndexUnchecked(i, j, 255) (src/cuda_compute/cuda_helper.cuh:97-104), i < j */
+static inline uint32_t tri_index(uint32_t i, uint32_t j)
+{
+    const uint32_t base = i * (2u * NPLATE - i - 1u) / 2u;
+    return base + (j - i - 1u);
+}
+
+/* ---- noise (vendored cudaNoise, src/cuda_compute/cuda_noise.cuh) ---------------------- */
+
+/* Robert Jenkins' 32-bit integer hash, as used by cuda_noise.cuh:44-54. */
+uint32_t or_hash(uint32_t a)
+{
+    a = (a + 0x7ed55d16u) + (a << 12);
+    a = (a ^ 0xc761c23cu) ^ (a >> 19);
+    a = (a + 0x165667b1u) + (a << 5);
+    a = (a + 0xd3a2646cu) ^ (a << 9);
+    a = (a + 0xfd7046c5u) + (a << 3);
+    a = (a ^ 0xb55a4f09u) ^ (a >> 16);
+    return a;
+}
+
+/* float -> u32 with the GPU's conversion semantics (truncate, saturate, NaN -> 0). */
+static inline uint32_t f2u_sat(float v)
+{
+    if (!(v > 0.0f)) return 0u;
+    if (v >= 4294967296.0f) return 0xffffffffu;
+    return (uint32_t)v;
+}
+
+/* randomFloat + randomGrid (cuda_noise.cuh:66-71, :108-111) */
+static float random_grid(int x, int y, int z, int seed)
+{
+    float v = (float)x * 1723.0f;
+    v = v + (float)y * 93241.0f;
+    v = v + (float)z * 149812.0f;
+    v = v + 3824.0f;
+    v = v + (float)seed;
+    const uint32_t hv = or_hash(f2u_sat(v));
+    const float r = (float)hv / 4294967296.0f; /* (float)0xffffffff */
+    return r * 2.0f - 1.0f;
+}
+
+/* discreteNoise(make_float3(x, 0, y), 1, seed) as called by rain (cuda_noise.cuh:470-477,
+ * plate_tectonics_kernel.cu:2434). */
+float or_rain_noise(int x, int y, int seed)
+{
+    const int ix = (int)((float)x * 1.0f);
+    const int iy = 0;
+    const int iz = (int)((float)y * 1.0f);
+    return random_grid(ix, iy, iz, seed);
+}
+
+/* Gustavson's 3D simplex gradient set, in the order of cuda_noise.cuh:158-160 */
+static const float GRAD3[12][3] = {
+    {1, 1, 0}, {-1, 1, 0}, {1, -1, 0}, {-1, -1, 0},
+    {1, 0, 1}, {-1, 0, 1}, {1, 0, -1}, {-1, 0, -1},
+    {0, 1, 1}, {0, -1, 1}, {0, 1, -1}, {0, -1, -1}};
+
+static inline float gdot(int g, float x, float y, float z)
+{
+    return (GRAD3[g][0] * x + GRAD3[g][1] * y) + GRAD3[g][2] * z;
+}
+
+static inline int perm12(uint32_t p) { return (int)(or_hash(p) % 12u); }
+
+/* simplexNoise (cuda_noise.cuh:228-320): Gustavson 3D simplex with hashed gradients. */
+float or_simplex3(float px, float py, float pz, float scale, int seed)
+{
+    const float xin = px * scale, yin = py * scale, zin = pz * scale;
+    const float F3 = 1.0f / 3.0f, G3 = 1.0f / 6.0f;
+    const float s = ((xin + yin) + zin) * F3;
+    const int i = (int)floorf(xin + s);
+    const int j = (int)floorf(yin + s);
+    const int k = (int)floorf(zin + s);
+    const float t = (float)(i + j + k) * G3;
+    const float X0 = (float)i - t, Y0 = (float)j - t, Z0 = (float)k - t;
+    const float x0 = xin - X0, y0 = yin - Y0, z0 = zin - Z0;
+    int i1, j1, k1, i2, j2, k2;
+    if (x0 >= y0) {
+        if (y0 >= z0) { i1 = 1; j1 = 0; k1 = 0; i2 = 1; j2 = 1; k2 = 0; }
+        else if (x0 >= z0) { i1 = 1; j1 = 0; k1 = 0; i2 = 1; j2 = 0; k2 = 1; }
+        else { i1 = 0; j1 = 0; k1 = 1; i2 = 1; j2 = 0; k2 = 1; }
+    } else {
+        if (y0 < z0) { i1 = 0; j1 = 0; k1 = 1; i2 = 0; j2 = 1; k2 = 1; }
+        else if (x0 < z0) { i1 = 0; j1 = 1; k1 = 0; i2 = 0; j2 = 1; k2 = 1; }
+        else { i1 = 0; j1 = 1; k1 = 0; i2 = 1; j2 = 1; k2 = 0; }
+    }
+    const float x1 = (x0 - (float)i1) + G3, y1 = (y0 - (float)j1) + G3, z1 = (z0 - (float)k1) + G3;
+    const float x2 = (x0 - (float)i2) + 2.0f * G3, y2 = (y0 - (float)j2) + 2.0f * G3,
+                z2 = (z0 - (float)k2) + 2.0f * G3;
+    const float x3 = (x0 - 1.0f) + 3.0f * G3, y3 = (y0 - 1.0f) + 3.0f * G3,
+                z3 = (z0 - 1.0f) + 3.0f * G3;
+    const uint32_t us = (uint32_t)seed, ui = (uint32_t)i, uj = (uint32_t)j, uk = (uint32_t)k;
+    const int gi0 = perm12(us + ui * 607495u + uj * 359609u + uk * 654846u);
+    const int gi1 = perm12(us + (ui + (uint32_t)i1) * 607495u + (uj + (uint32_t)j1) * 359609u +
+                           (uk + (uint32_t)k1) * 654846u);
+    const int gi2 = perm12(us + (ui + (uint32_t)i2) * 607495u + (uj + (uint32_t)j2) * 359609u +
+                           (uk + (uint32_t)k2) * 654846u);
+    const int gi3 = perm12(us + (ui + 1u) * 607495u + (uj + 1u) * 359609u + (uk + 1u) * 654846u);
+    float n0, n1, n2, n3;
+    float t0 = ((0.6f - x0 * x0) - y0 * y0) - z0 * z0;
+    if (t0 < 0.0f) n0 = 0.0f; else { t0 = t0 * t0; n0 = (t0 * t0) * gdot(gi0, x0, y0, z0); }
+    float t1 = ((0.6f - x1 * x1) - y1 * y1) - z1 * z1;
+    if (t1 < 0.0f) n1 = 0.0f; else { t1 = t1 * t1; n1 = (t1 * t1) * gdot(gi1, x1, y1, z1); }
+    float t2 = ((0.6f - x2 * x2) - y2 * y2) - z2 * z2;
+    if (t2 < 0.0f) n2 = 0.0f; else { t2 = t2 * t2; n2 = (t2 * t2) * gdot(gi2, x2, y2, z2); }
+    float t3 = ((0.6f - x3 * x3) - y3 * y3) - z3 * z3;
+    if (t3 < 0.0f) n3 = 0.0f; else { t3 = t3 * t3; n3 = (t3 * t3) * gdot(gi3, x3, y3, z3); }
+    return 32.0f * (((n0 + n1) + n2) + n3);
+}
+
+/* cuda::std::lerp (P0811R3 algorithm), used by processDivergence (plate_tectonics_kernel.cu:354) */
+float or_lerp(float a, float b, float t)
+{
+    if ((a <= 0.0f && b >= 0.0f) || (a >= 0.0f && b <= 0.0f)) return t * b + (1.0f - t) * a;
+    if (t == 1.0f) return b;
+    const float x = a + t * (b - a);
+    if ((t > 1.0f) == (b > a)) return b < x ? x : b;
+    return x < b ? x : b;
+}
+
+/* The engine's sine (include/tecto_math.h) by default; libm's sinf when pinning against the
+ * reference's kernels compiled for the CPU, which call the host sinf. */
+static int g_libm_sin = 0;
+void or_use_libm_sin(int on) { g_libm_sin = on; }
+float or_sinf(float x) { return g_libm_sin ? sinf(x) : tecto_sinf(x); }
+
+/* ---- plate kinematics ------------------------------------------------------------------ */
+
+/* getPixelMovements' integer displacement (plate_tectonics_kernel.cu:248-257) and the sub-cell
+ * centre update of applyPlateMovementChanges (:1871-1878). */
+void or_plate_offsets(const tecto_plate *p, int32_t *off_x, int32_t *off_y, tecto_plate *next)
+{
+    for (unsigned k = 0; k < NPLATE; ++k) {
+        const float mx = p[k].direction_x * p[k].velocity;
+        const float my = p[k].direction_y * p[k].velocity;
+        const float cx = p[k].pixelCenter_x + mx;
+        const float cy = p[k].pixelCenter_y + my;
+        const float fx = floorf(cx), fy = floorf(cy);
+        off_x[k] = (int32_t)fx;
+        off_y[k] = (int32_t)fy;
+        if (next) {
+            next[k] = p[k];
+            next[k].pixelCenter_x = cx - fx;
+            next[k].pixelCenter_y = cy - fy;
+        }
+    }
+}
+
+/* ---- advection + grouping --------------------------------------------------------------- */
+
+/* getPixelMovements (plate_tectonics_kernel.cu:232-271) and registerPlateCollisions
+ * (:273-298) with arrivals taken in ascending source order (the stable sort's order). */
+void or_collision_words(int W, int H, const uint8_t *id, const int32_t *off_x, const int32_t *off_y,
+                        uint32_t *dest, uint32_t *word, uint32_t *sorted_keys, uint32_t *sorted_vals)
+{
+    const size_t N = (size_t)W * (size_t)H;
+    uint32_t *d = dest ? dest : (uint32_t *)malloc(N * sizeof(uint32_t));
+    uint32_t *cnt = (uint32_t *)calloc(N + 1, sizeof(uint32_t));
+    for (size_t i = 0; i < N; ++i) {
+        const int x = (int)(i % (size_t)W), y = (int)(i / (size_t)W);
+        const uint8_t p = id[i];
+        d[i] = cidx(x + off_x[p], y + off_y[p], W, H);
+    }
+    if (word) {
+        memset(word, 0, N * sizeof(uint32_t));
+        for (size_t i = 0; i < N; ++i) {
+            const uint32_t k = cnt[d[i]]++;
+            if (k < 4u) word[d[i]] |= (uint32_t)(255u - id[i]) << (8u * k);
+        }
+    } else {
+        for (size_t i = 0; i < N; ++i) cnt[d[i]]++;
+    }
+    if (sorted_keys || sorted_vals) {
+        /* counting sort: exclusive prefix of arrival counts, then a stable scatter */
+        uint32_t run = 0;
+        for (size_t c = 0; c < N; ++c) { const uint32_t v = cnt[c]; cnt[c] = run; run += v; }
+        for (size_t i = 0; i < N; ++i) {
+            const uint32_t pos = cnt[d[i]]++;
+            if (sorted_keys) sorted_keys[pos] = d[i];
+            if (sorted_vals) sorted_vals[pos] = (uint32_t)i;
+        }
+    }
+    free(cnt);
+    if (!dest) free(d);
+}
+
+/* ---- collision typing ------------------------------------------------------------------- */
+
+typedef struct { int32_t c[5]; } pair_counts; /* CollisionTypeCounts field order,
+                                                 plate_tectonics_kernel.cuh:47-54 */
+
+/* writeCollision (plate_tectonics_kernel.cu:794-836), including the as-compiled early-exit test
+ * `packed >> 0 & 1 && packed >> 4 & 0x0F < cooldown` == `(packed & 1) && ((packed >> 4) &
+ * (15 < cooldown))` (:813). */
+static void write_collision(float hA, float hB, uint8_t A, uint8_t B, const uint8_t *bm,
+                            pair_counts *counts, const tecto_kernel_settings *ks)
+{
+    const int cond = A < B;
+    const uint8_t mn = cond ? A : B, mx = cond ? B : A;
+    const float mnH = cond ? hA : hB, mxH = cond ? hB : hA;
+    const uint32_t idx = tri_index(mn, mx);
+    const uint8_t packed = bm[idx];
+    if ((packed & 1u) && ((packed >> 4) & (uint32_t)(0x0F < ks->collisionTypeUpdateCooldown)))
+        return;
+    const int minCont = mnH >= ks->continentalCrustThreshold;
+    const int maxCont = mxH >= ks->continentalCrustThreshold;
+    if (minCont && maxCont) counts[idx].c[4]++;
+    else if (minCont) counts[idx].c[2]++;
+    else if (maxCont) counts[idx].c[0]++;
+    else if (mnH <= mxH) counts[idx].c[1]++;
+    else counts[idx].c[3]++;
+}
+
+/* determineCollisionType kernel (plate_tectonics_kernel.cu:838-888) and
+ * createCollisionTypeMatrix (:890-972). */
+void or_collision_types(int W, int H, const uint32_t *word, const float *h_old, const int32_t *off_x,
+                        const int32_t *off_y, const tecto_kernel_settings *ks, uint8_t *bm)
+{
+    const size_t N = (size_t)W * (size_t)H;
+    pair_counts *counts = (pair_counts *)calloc(TECTO_NUM_PAIRS, sizeof(pair_counts));
+    for (size_t d = 0; d < N; ++d) {
+        const uint32_t cp = word[d];
+        if (cp <= 0xFFu) continue;
+        const uint8_t A = (uint8_t)(255u - (cp & 0xFFu));
+        const uint8_t B = (uint8_t)(255u - ((cp >> 8) & 0xFFu));
+        const uint8_t C = (uint8_t)(255u - ((cp >> 16) & 0xFFu));
+        const uint8_t D = (uint8_t)(255u - ((cp >> 24) & 0xFFu));
+        const int x = (int)(d % (size_t)W), y = (int)(d / (size_t)W);
+        /* determineCollisionHeight (:781-792): height at the arrival's source cell */
+        const float hA = h_old[cidx(x - off_x[A], y - off_y[A], W, H)];
+        const float hB = h_old[cidx(x - off_x[B], y - off_y[B], W, H)];
+        if (D != NPLATE) {
+            const float hC = h_old[cidx(x - off_x[C], y - off_y[C], W, H)];
+            const float hD = h_old[cidx(x - off_x[D], y - off_y[D], W, H)];
+            write_collision(hA, hB, A, B, bm, counts, ks);
+            write_collision(hA, hC, A, C, bm, counts, ks);
+            write_collision(hA, hD, A, D, bm, counts, ks);
+            write_collision(hB, hC, B, C, bm, counts, ks);
+            write_collision(hB, hD, B, D, bm, counts, ks);
+            write_collision(hC, hD, C, D, bm, counts, ks);
+        } else if (C != NPLATE) {
+            const float hC = h_old[cidx(x - off_x[C], y - off_y[C], W, H)];
+            write_collision(hA, hB, A, B, bm, counts, ks);
+            write_collision(hA, hC, A, C, bm, counts, ks);
+            write_collision(hB, hC, B, C, bm, counts, ks);
+        } else {
+            write_collision(hA, hB, A, B, bm, counts, ks);
+        }
+    }
+    for (uint32_t idx = 0; idx < TECTO_NUM_PAIRS; ++idx) {
+        const uint32_t packed = bm[idx];
+        const int hasType = packed & 1u;
+        const int count = (int)((packed >> 4) & 0x0Fu);
+        const int32_t *c = counts[idx].c;
+        const uint32_t total = (uint32_t)(c[0] + c[1] + c[2] + c[3] + c[4]);
+        if (total == 0) continue;
+        if (hasType && count < ks->collisionTypeUpdateCooldown) {
+            bm[idx] = (uint8_t)((packed & 0x0Fu) | (((uint32_t)(count + 1) & 0x0Fu) << 4));
+            continue;
+        }
+        if (total < (uint32_t)ks->minCollisionSize) continue;
+        uint32_t out = packed & 0x0Fu;
+        const int hasPol = (packed >> 2) & 1u;
+        const int polA = (packed >> 3) & 1u;
+        const int oppA = c[2] + c[4], oppB = c[0] + c[4];
+        const int subA = c[0] + c[1] - oppA, subB = c[2] + c[3] - oppB;
+        if (c[4] >= c[0] + c[1] && c[4] >= c[2] + c[3]) out |= 3u;
+        else if (subA > 0 && subA > subB && (!hasPol || polA)) out = (out & ~2u) | 13u;
+        else if (subB > 0 && subB > subA && (!hasPol || !polA)) out = (out & ~10u) | 5u;
+        bm[idx] = (uint8_t)out;
+    }
+    free(counts);
+}
+
+/* determineCollisionType device function (plate_tectonics_kernel.cu:611-649) */
+static uint32_t pair_type(const uint8_t *bm, uint8_t A, uint8_t B, float hA, float hB,
+                          const tecto_kernel_settings *ks)
+{
+    const int cond = A < B;
+    const uint8_t mn = cond ? A : B, mx = cond ? B : A;
+    const float mnH = cond ? hA : hB, mxH = cond ? hB : hA;
+    const uint8_t packed = bm[tri_index(mn, mx)];
+    const int hasType = packed & 1u, type = (packed >> 1) & 1u, pol = (packed >> 3) & 1u;
+    uint32_t out = 0;
+    if (hasType && type == 0) {
+        if (pol == 1) {
+            if (mnH >= ks->continentalCrustThreshold) out = mn == A ? 3u : 4u;
+            else out = mn == A ? 1u : 2u;
+        }
+        if (pol == 0) {
+            if (mxH >= ks->continentalCrustThreshold) out = mx == A ? 3u : 4u;
+            else out = mx == A ? 1u : 2u;
+        }
+    }
+    return out;
+}
+
+/* ---- resolve ------------------------------------------------------------------------------ */
+
+void or_gaussian_weights(float sigma, int radius, float *w_out)
+{
+    double tmp[17];
+    double sum = 0.0;
+    for (int k = -radius; k <= radius; ++k) {
+        tmp[k + radius] = exp(-(double)(k * k) / (2.0 * (double)sigma * (double)sigma));
+        sum += tmp[k + radius];
+    }
+    for (int k = 0; k <= 2 * radius; ++k) w_out[k] = (float)(tmp[k] / sum);
+}
+
+void or_resolve(int W, int H, const uint8_t *id_old, const float *h_old, const uint32_t *word,
+                const int32_t *off_x, const int32_t *off_y, const uint8_t *bm, uint32_t *div_bitmap,
+                const tecto_settings *st, uint32_t seed, uint32_t iteration, float *h_new,
+                uint8_t *id_new, uint8_t *acc)
+{
+    const tecto_kernel_settings *ks = &st->kernel;
+    const size_t N = (size_t)W * (size_t)H;
+    uint32_t has_div[TECTO_NUM_DIV_WORDS];
+    memset(has_div, 0, sizeof(has_div));
+    memset(acc, 0, N);
+    static const int PL[6][2] = {{0, 1}, {0, 2}, {1, 2}, {0, 3}, {1, 3}, {2, 3}};
+
+    /* processCollisions (plate_tectonics_kernel.cu:677-745); cells in ascending order, so a later
+     * accretion mark overwrites an earlier one exactly as a sequential launch would. */
+    for (size_t d = 0; d < N; ++d) {
+        const int x = (int)(d % (size_t)W), y = (int)(d / (size_t)W);
+        const uint32_t cv = word[d];
+        if (cv == 0) {
+            /* processDivergence (:301-362) */
+            const uint8_t prev = id_old[d];
+            const uint32_t opp = cidx(x - off_x[prev], y - off_y[prev], W, H);
+            const uint32_t cvo = word[opp];
+            const uint8_t oppId = (uint8_t)((255u - cvo) & 0xFFu);
+            uint8_t nid;
+            if (cvo != 0 && cvo <= 0xFFu && oppId != prev) {
+                const uint8_t mn = prev < oppId ? prev : oppId;
+                const uint8_t mx = prev < oppId ? oppId : prev;
+                const uint32_t bit = tri_index(mn, mx);
+                nid = (div_bitmap[bit / 32u] & (1u << (bit % 32u))) ? mn : mx;
+                has_div[bit / 32u] |= 1u << (bit % 32u);
+            } else {
+                nid = prev;
+            }
+            const float noise = or_simplex3((float)x, (float)y, (float)iteration, 0.01f, (int)seed);
+            const float target = ks->divergence_height_target_min +
+                                 noise * (ks->divergence_height_target_max -
+                                          ks->divergence_height_target_min);
+            h_new[d] = or_lerp(h_old[d], target, ks->divergence_interpolation_factor);
+            id_new[d] = nid;
+            continue;
+        }
+        uint8_t ids[4];
+        for (int k = 0; k < 4; ++k) ids[k] = (uint8_t)(255u - ((cv >> (8 * k)) & 0xFFu));
+        if (ids[1] == NPLATE) {
+            /* processMovement (:586-609) */
+            const uint8_t p = ids[0];
+            id_new[d] = p;
+            h_new[d] = h_old[cidx(x - off_x[p], y - off_y[p], W, H)];
+            continue;
+        }
+        /* processConvergence (:469-584) */
+        const int n = ids[3] != NPLATE ? 4 : ids[2] != NPLATE ? 3 : 2;
+        const int pairLen = n == 4 ? 6 : n == 3 ? 3 : 1;
+        float heights[4] = {0, 0, 0, 0};
+        for (int k = 0; k < n; ++k)
+            heights[k] = h_old[cidx(x - off_x[ids[k]], y - off_y[ids[k]], W, H)];
+        uint32_t types[6];
+        for (int a = 0; a < pairLen; ++a)
+            types[a] = pair_type(bm, ids[PL[a][0]], ids[PL[a][1]], heights[PL[a][0]],
+                                 heights[PL[a][1]], ks);
+        int sub[4] = {0, 0, 0, 0};
+        for (int a = 0; a < pairLen; ++a) {
+            if (types[a] == 1 || types[a] == 3) sub[PL[a][0]] = 1;
+            else if (types[a] == 2 || types[a] == 4) sub[PL[a][1]] = 1;
+        }
+        int owner = 0;
+        for (int i = 0; i < n; ++i)
+            if (!sub[i]) owner = i;
+        const uint8_t ownerId = ids[owner];
+        float writeH = heights[owner];
+        for (int a = 0; a < pairLen; ++a) {
+            const int ia = PL[a][0], ib = PL[a][1];
+            float hh;
+            if (ia == owner) hh = heights[ib];
+            else if (ib == owner) hh = heights[ia];
+            else continue;
+            if (hh > writeH) { const float tmp = hh; hh = writeH; writeH = tmp; }
+            const uint32_t t = types[a];
+            int other = -1;
+            if (ia == owner && t == 4) other = ib;
+            else if (ib == owner && t == 3) other = ia;
+            if (other >= 0) {
+                const uint8_t po = ids[other];
+                uint32_t target;
+                if (off_x[po] != 0 || off_y[po] != 0)
+                    target = cidx(x - off_x[po], y - off_y[po], W, H);
+                else
+                    target = cidx(x + off_x[ownerId], y + off_y[ownerId], W, H);
+                acc[target] = (uint8_t)(255u - ownerId);
+            }
+        }
+        h_new[d] = writeH;
+        id_new[d] = ownerId;
+    }
+    /* flipDivergedBitmap (:772-780) */
+    for (int i = 0; i < TECTO_NUM_DIV_WORDS; ++i) div_bitmap[i] ^= has_div[i];
+
+    /* Gaussian uplift: upliftAmount on convergent cells, separable blur (x then y), added. */
+    if (st->step.upliftMode == TECTO_UPLIFT_GAUSSIAN) {
+        const int r = st->step.upliftRadius;
+        float wts[17];
+        or_gaussian_weights(st->step.upliftSigma, r, wts);
+        const float amount = st->step.upliftAmount;
+        float *tmp = (float *)malloc(N * sizeof(float));
+#pragma omp parallel for schedule(static)
+        for (int y = 0; y < H; ++y)
+            for (int x = 0; x < W; ++x) {
+                float a = 0.0f;
+                for (int k = -r; k <= r; ++k) {
+                    const float u = word[cidx(x + k, y, W, H)] > 0xFFu ? amount : 0.0f;
+                    a = a + wts[k + r] * u;
+                }
+                tmp[(size_t)y * W + x] = a;
+            }
+#pragma omp parallel for schedule(static)
+        for (int y = 0; y < H; ++y)
+            for (int x = 0; x < W; ++x) {
+                float a = 0.0f;
+                for (int k = -r; k <= r; ++k) a = a + wts[k + r] * tmp[cidx(x, y + k, W, H)];
+                h_new[(size_t)y * W + x] = h_new[(size_t)y * W + x] + a;
+            }
+        free(tmp);
+    }
+}
+
+/* ---- thermal ------------------------------------------------------------------------------- */
+
+static const int TH_DX[8] = {-1, 1, 0, 0, -1, -1, 1, 1};
+static const int TH_DY[8] = {0, 0, -1, 1, -1, 1, -1, 1};
+
+/* thermalErosionKernel (plate_tectonics_kernel.cu:2735-2786) in gather form. */
+void or_thermal(int W, int H, float *h, int iters, const tecto_kernel_settings *ks)
+{
+    const size_t N = (size_t)W * (size_t)H;
+    const float thr = ks->thermalThresholdAngle * ks->thermalCellSize;
+    const float A = ks->thermalErosionAmplitude, S = ks->thermalErosionStrength;
+    float *tot = (float *)malloc(N * sizeof(float));
+    float *hn = (float *)malloc(N * sizeof(float));
+    for (int it = 0; it < iters; ++it) {
+#pragma omp parallel for schedule(static)
+        for (int y = 0; y < H; ++y)
+            for (int x = 0; x < W; ++x) {
+                const float hc = h[(size_t)y * W + x];
+                float t = 0.0f;
+                for (int d = 0; d < 8; ++d) {
+                    const float diff = hc - h[cidx(x + TH_DX[d], y + TH_DY[d], W, H)];
+                    if (diff > thr) t = t + diff;
+                }
+                tot[(size_t)y * W + x] = t;
+            }
+#pragma omp parallel for schedule(static)
+        for (int y = 0; y < H; ++y)
+            for (int x = 0; x < W; ++x) {
+                const size_t i = (size_t)y * W + x;
+                const float hc = h[i];
+                float v = hc;
+                if (tot[i] > 0.0f)
+                    for (int d = 0; d < 8; ++d) {
+                        const float diff = hc - h[cidx(x + TH_DX[d], y + TH_DY[d], W, H)];
+                        if (diff > thr) v = v - (A * (diff / tot[i])) * S;
+                    }
+                for (int d = 0; d < 8; ++d) {
+                    const uint32_t nb = cidx(x + TH_DX[d], y + TH_DY[d], W, H);
+                    const float diff = h[nb] - hc;
+                    if (diff > thr && tot[nb] > 0.0f) v = v + (A * (diff / tot[nb])) * S;
+                }
+                hn[i] = v;
+            }
+        memcpy(h, hn, N * sizeof(float));
+    }
+    free(tot);
+    free(hn);
+}
+
+/* ---- hydraulic ----------------------------------------------------------------------------- */
+
+/* applyHydraulicErosion (plate_tectonic_sim.cu:331-373): per sub-iteration rain, flux, flow,
+ * sediment (slope from a copy of the height), transport, evaporate; kernels at
+ * plate_tectonics_kernel.cu:2430-2593. */
+void or_hydraulic(int W, int H, float *h, float *w, float *s, float *flux, int iters, float dt,
+                  uint32_t rain_seed, const tecto_kernel_settings *ks)
+{
+    const size_t N = (size_t)W * (size_t)H;
+    float *fl = (float *)malloc(N * 4 * sizeof(float));  /* new flux */
+    float *vx = (float *)malloc(N * sizeof(float));
+    float *vy = (float *)malloc(N * sizeof(float));
+    float *hc = (float *)malloc(N * sizeof(float));       /* height copy */
+    float *s2 = (float *)malloc(N * sizeof(float));
+    const int seed = (int)rain_seed;
+    const float A = ks->hydrationPipeCrossSection, L = ks->hydrationPipeLength, G = ks->gravity;
+    for (int it = 0; it < iters; ++it) {
+        /* rain (:2430-2437) */
+#pragma omp parallel for schedule(static)
+        for (int y = 0; y < H; ++y)
+            for (int x = 0; x < W; ++x) {
+                const size_t i = (size_t)y * W + x;
+                w[i] = w[i] + (fmaxf(0.0f, or_rain_noise(x, y, seed)) * dt) * ks->hydrationRainfall;
+            }
+        /* flux (:2439-2485) */
+#pragma omp parallel for schedule(static)
+        for (int y = 0; y < H; ++y)
+            for (int x = 0; x < W; ++x) {
+                const size_t i = (size_t)y * W + x;
+                const int nx[4] = {x - 1, x, x + 1, x};
+                const int ny[4] = {y, y + 1, y, y - 1};
+                float o[4];
+                for (int k = 0; k < 4; ++k) {
+                    const uint32_t n = cidx(nx[k], ny[k], W, H);
+                    const float dh = ((h[i] + w[i]) - h[n]) - w[n];
+                    o[k] = fmaxf(0.0f, flux[4 * i + k] + (dt * A) * ((G * dh) / L));
+                }
+                const float total = (((o[0] + o[1]) + o[2]) + o[3]) + 1e-6f;
+                float K = fminf(1.0f, w[i] / (total * dt + 1e-6f));
+                K = fmaxf(K, 0.01f);
+                for (int k = 0; k < 4; ++k) fl[4 * i + k] = o[k] * K;
+            }
+        /* flow (:2487-2533); the flux texture is replaced by the new flux */
+#pragma omp parallel for schedule(static)
+        for (int y = 0; y < H; ++y)
+            for (int x = 0; x < W; ++x) {
+                const size_t i = (size_t)y * W + x;
+                const float *fL = fl + 4 * (size_t)cidx(x - 1, y, W, H);
+                const float *fU = fl + 4 * (size_t)cidx(x, y + 1, W, H);
+                const float *fR = fl + 4 * (size_t)cidx(x + 1, y, W, H);
+                const float *fD = fl + 4 * (size_t)cidx(x, y - 1, W, H);
+                const float *fC = fl + 4 * i;
+                float in = 0.0f;
+                in = in + fL[2];
+                in = in + fU[3];
+                in = in + fR[0];
+                in = in + fD[1];
+                const float out = ((fC[0] + fC[1]) + fC[2]) + fC[3];
+                const float dv = dt * (in - out);
+                const float wn = fmaxf(0.0f, w[i] + dv);
+                w[i] = wn;
+                const float nfx = (((fL[2] - fC[0]) + fC[2]) - fR[0]) * 0.5f;
+                const float nfy = (((fU[3] - fC[1]) + fC[1]) - fD[3]) * 0.5f;
+                const float hh = fmaxf(wn, 0.01f);
+                float ux = nfx / hh, uy = nfy / hh;
+                const float mag = sqrtf(ux * ux + uy * uy);
+                if (mag > 50.0f) {
+                    const float sc = 50.0f / mag;
+                    ux = ux * sc;
+                    uy = uy * sc;
+                }
+                vx[i] = ux;
+                vy[i] = uy;
+            }
+        memcpy(flux, fl, N * 4 * sizeof(float));
+        memcpy(hc, h, N * sizeof(float));
+        /* sediment (:2535-2570), slope of the height copy (cuda_texture.cuh:78-89) */
+#pragma omp parallel for schedule(static)
+        for (int y = 0; y < H; ++y)
+            for (int x = 0; x < W; ++x) {
+                const size_t i = (size_t)y * W + x;
+                const float dzdx = (hc[cidx(x + 1, y, W, H)] - hc[cidx(x - 1, y, W, H)]) * 0.5f;
+                const float dzdy = (hc[cidx(x, y + 1, W, H)] - hc[cidx(x, y - 1, W, H)]) * 0.5f;
+                const float slope = sqrtf(dzdx * dzdx + dzdy * dzdy);
+                const float mag = sqrtf(vx[i] * vx[i] + vy[i] * vy[i]);
+                float C = (ks->sedimentCapacity * or_sinf(fmaxf(slope, 0.03f))) * mag;
+                C = fminf(C, 5.0f);
+                const float sd = s[i];
+                if (C > sd) {
+                    float e = (ks->sedimentErosionRate * (C - sd)) * dt;
+                    e = fminf(e, hc[i]);
+                    h[i] = hc[i] - e;
+                    s[i] = sd + e;
+                } else {
+                    float dd = (ks->sedimentDepositionRate * (sd - C)) * dt;
+                    dd = fminf(dd, sd);
+                    s[i] = sd - dd;
+                    h[i] = hc[i] + dd;
+                }
+            }
+        /* transport (:2572-2585): bilinear sample with wrap (cuda_helper.cuh:48-65) */
+#pragma omp parallel for schedule(static)
+        for (int y = 0; y < H; ++y)
+            for (int x = 0; x < W; ++x) {
+                const size_t i = (size_t)y * W + x;
+                const float px = (float)x - vx[i] * dt;
+                const float py = (float)y - vy[i] * dt;
+                const int x0 = (int)floorf(px), y0 = (int)floorf(py);
+                const int x1 = x0 + 1, y1 = y0 + 1;
+                const float wx = px - (float)x0, wy = py - (float)y0;
+                const float I0 = (1.0f - wx) * s[cidx(x0, y0, W, H)] + wx * s[cidx(x1, y0, W, H)];
+                const float I1 = (1.0f - wx) * s[cidx(x0, y1, W, H)] + wx * s[cidx(x1, y1, W, H)];
+                s2[i] = (1.0f - wy) * I0 + wy * I1;
+            }
+        memcpy(s, s2, N * sizeof(float));
+        /* evaporate (:2587-2593) */
+#pragma omp parallel for schedule(static)
+        for (size_t i = 0; i < N; ++i)
+            w[i] = fmaxf(0.0f, w[i] - (fminf(w[i], 20.0f) * ks->hydrationEvaporation) * dt);
+    }
+    free(fl);
+    free(vx);
+    free(vy);
+    free(hc);
+    free(s2);
+}
+
+/* ---- accretion ------------------------------------------------------------------------------ */
+
+/* applyAccretion (plate_tectonics_kernel.cu:747-770) */
+void or_accretion(int W, int H, const float *h, const uint8_t *acc, uint8_t *id,
+                  const tecto_kernel_settings *ks)
+{
+    const size_t N = (size_t)W * (size_t)H;
+    for (size_t i = 0; i < N; ++i) {
+        const uint8_t a = (uint8_t)(255u - acc[i]);
+        if (a == NPLATE) continue;
+        if (h[i] >= ks->continentalCrustThreshold) id[i] = a;
+    }
+}
+
+/* ---- CCL ------------------------------------------------------------------------------------ */
+
+static uint32_t uf_find(uint32_t *p, uint32_t a)
+{
+    while (p[a] != a) {
+        p[a] = p[p[a]];
+        a = p[a];
+    }
+    return a;
+}
+
+static void uf_union(uint32_t *p, uint32_t a, uint32_t b)
+{
+    a = uf_find(p, a);
+    b = uf_find(p, b);
+    if (a < b) p[b] = a;
+    else if (b < a) p[a] = b;
+}
+
+/* Connected components of equal plate id on the torus (ccl.cu:35-177).  Modes 4 and 8 are the
+ * true 4- and 8-neighbourhoods; TECTO_CCL_REF8 is the union set the reference's kernels build:
+ * init's single link to the first equal of (tl, t, tr, l) (ccl.cu:107-116), reduce's l and tl
+ * unions on every row and t and tr unions on row 0 (ccl.cu:157-176).  Labels = minimum index. */
+void or_ccl(int W, int H, const uint8_t *id, uint32_t *labels, int mode)
+{
+    const size_t N = (size_t)W * (size_t)H;
+    for (size_t i = 0; i < N; ++i) labels[i] = (uint32_t)i;
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const uint32_t i = (uint32_t)((size_t)y * W + x);
+            const uint8_t c = id[i];
+            const uint32_t l = cidx(x - 1, y, W, H), t = cidx(x, y - 1, W, H);
+            const uint32_t tl = cidx(x - 1, y - 1, W, H), tr = cidx(x + 1, y - 1, W, H);
+            if (mode == TECTO_CCL_4) {
+                if (id[l] == c) uf_union(labels, i, l);
+                if (id[t] == c) uf_union(labels, i, t);
+            } else if (mode == TECTO_CCL_8) {
+                if (id[l] == c) uf_union(labels, i, l);
+                if (id[t] == c) uf_union(labels, i, t);
+                if (id[tl] == c) uf_union(labels, i, tl);
+                if (id[tr] == c) uf_union(labels, i, tr);
+            } else {
+                if (id[tl] == c) uf_union(labels, i, tl);
+                else if (id[t] == c) uf_union(labels, i, t);
+                else if (id[tr] == c) uf_union(labels, i, tr);
+                else if (id[l] == c) uf_union(labels, i, l);
+                if (y == 0) {
+                    if (id[t] == c) uf_union(labels, i, t);
+                    if (id[tr] == c) uf_union(labels, i, tr);
+                }
+                if (id[tl] == c) uf_union(labels, i, tl);
+                if (id[l] == c) uf_union(labels, i, l);
+            }
+        }
+    for (size_t i = 0; i < N; ++i) labels[i] = uf_find(labels, (uint32_t)i);
+}
+
+/* ---- full step ---------------------------------------------------------------------------- */
+
+/* PlateTectonicSim::executeIteration (plate_tectonic_sim.cu:54-131), hot-path phases. */
+void or_step(int W, int H, float *h, float *w, float *s, float *flux, uint8_t *id, uint32_t *labels,
+             uint32_t *word, uint8_t *acc, uint8_t *bm, uint32_t *div_bitmap, tecto_plate *plates,
+             const tecto_settings *st, uint32_t seed, uint32_t *iteration)
+{
+    const size_t N = (size_t)W * (size_t)H;
+    int32_t offx[NPLATE], offy[NPLATE];
+    tecto_plate next[NPLATE];
+    or_plate_offsets(plates, offx, offy, next);
+    or_collision_words(W, H, id, offx, offy, NULL, word, NULL, NULL);
+    or_collision_types(W, H, word, h, offx, offy, &st->kernel, bm);
+    float *hn = (float *)malloc(N * sizeof(float));
+    uint8_t *idn = (uint8_t *)malloc(N);
+    or_resolve(W, H, id, h, word, offx, offy, bm, div_bitmap, st, seed, *iteration, hn, idn, acc);
+    memcpy(h, hn, N * sizeof(float));
+    memcpy(id, idn, N);
+    free(hn);
+    free(idn);
+    or_thermal(W, H, h, st->step.thermalIterations, &st->kernel);
+    or_hydraulic(W, H, h, w, s, flux, st->step.hydraulicIterations, st->step.hydraulicDt,
+                 seed + *iteration, &st->kernel);
+    or_accretion(W, H, h, acc, id, &st->kernel);
+    memcpy(plates, next, sizeof(next));
+    const int period = st->sim.iterationsForCCL > 0 ? st->sim.iterationsForCCL : 1;
+    if (*iteration % (uint32_t)period == 0) or_ccl(W, H, id, labels, st->step.cclConnectivity);
+    *iteration += 1;
+}

@@ -1,0 +1,86 @@
+/*
+ * tecto_oracle.h - CPU oracle for the plate-tectonics step.  TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C restatement of the reference's hot-path kernels (MarWo22/master_thesis,
+ * src/cuda_compute/), one function per phase, each citing the reference lines it follows.
+ * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load it; the engine
+ * (master_thesis_gb300/) never does.
+ *
+ * Arithmetic: IEEE single precision in the reference's expression order, no multiply-add
+ * contraction (built with -ffp-contract=off), sin from include/tecto_math.h.  Pinned against the
+ * reference kernels themselves, compiled for the CPU from their own sources by oracle/Makefile
+ * (target `ref`) and run with a sequential thread emulation (tests/golden/).
+ *
+ * Where the reference is order-dependent the oracle fixes one order, which the engine shares:
+ *  - arrival slots at a destination cell: ascending source linear index (a stable sort);
+ *  - accretion marks that hit the same cell: the mark of the highest destination index wins;
+ *  - thermal erosion: Jacobi (gather) form, own outflows subtracted in direction order, then
+ *    inflows added in direction order.
+ */
+#ifndef TECTO_ORACLE_H
+#define TECTO_ORACLE_H
+
+#include <stdint.h>
+#include "../include/tecto.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Per-plate integer displacement of this step and the updated sub-cell centres. */
+void or_plate_offsets(const tecto_plate *plates, int32_t *off_x, int32_t *off_y,
+                      tecto_plate *plates_next);
+
+/* Advection + canonical grouping: dest[i] for every cell, packed arrival words, and the
+ * stably sorted (dest, src) pairs (any output may be NULL). */
+void or_collision_words(int W, int H, const uint8_t *id, const int32_t *off_x, const int32_t *off_y,
+                        uint32_t *dest, uint32_t *word, uint32_t *sorted_keys,
+                        uint32_t *sorted_vals);
+
+/* Collision-type evidence + pair bitmap update (type_bitmap in/out). */
+void or_collision_types(int W, int H, const uint32_t *word, const float *h_old,
+                        const int32_t *off_x, const int32_t *off_y,
+                        const tecto_kernel_settings *ks, uint8_t *type_bitmap);
+
+/* processCollisions + flipDivergedBitmap + uplift.  div_bitmap in/out; acc receives accretion
+ * marks (zeroed first).  seed/iteration are the world's seed and step counter. */
+void or_resolve(int W, int H, const uint8_t *id_old, const float *h_old, const uint32_t *word,
+                const int32_t *off_x, const int32_t *off_y, const uint8_t *type_bitmap,
+                uint32_t *div_bitmap, const tecto_settings *st, uint32_t seed, uint32_t iteration,
+                float *h_new, uint8_t *id_new, uint8_t *acc);
+
+/* Thermal erosion, `iters` gather iterations, in place. */
+void or_thermal(int W, int H, float *h, int iters, const tecto_kernel_settings *ks);
+
+/* Hydraulic erosion, `iters` sub-iterations of step dt, in place; flux is 4 floats per cell. */
+void or_hydraulic(int W, int H, float *h, float *w, float *s, float *flux, int iters, float dt,
+                  uint32_t rain_seed, const tecto_kernel_settings *ks);
+
+/* applyAccretion, in place on id. */
+void or_accretion(int W, int H, const float *h, const uint8_t *acc, uint8_t *id,
+                  const tecto_kernel_settings *ks);
+
+/* CCL labels (TECTO_CCL_4 / _8 / _REF8), each the minimum linear index of its component. */
+void or_ccl(int W, int H, const uint8_t *id, uint32_t *labels, int mode);
+
+/* One full step.  Buffers are the world's state and are updated in place; word/acc/labels are
+ * outputs (labels only written on CCL steps). *iteration is advanced. */
+void or_step(int W, int H, float *h, float *w, float *s, float *flux, uint8_t *id,
+             uint32_t *labels, uint32_t *word, uint8_t *acc, uint8_t *type_bitmap,
+             uint32_t *div_bitmap, tecto_plate *plates, const tecto_settings *st, uint32_t seed,
+             uint32_t *iteration);
+
+/* Building blocks exposed for unit tests. */
+uint32_t or_hash(uint32_t v);
+float or_simplex3(float x, float y, float z, float scale, int seed);
+float or_rain_noise(int x, int y, int seed);
+float or_lerp(float a, float b, float t);
+void or_gaussian_weights(float sigma, int radius, float *w_out);
+float or_sinf(float x);
+void or_use_libm_sin(int on);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TECTO_ORACLE_H */

@@ -1,0 +1,163 @@
+"""Generate the golden vectors that pin the CPU oracle to the reference's own kernels.
+
+Runs here, where the reference sources exist: `make -C oracle ref` compiles the reference's
+hot-path kernels (MarWo22/master_thesis src/cuda_compute/plate_tectonics_kernel.cu, ccl.cu,
+kernel_settings.cu) for the CPU, and oracle/ref_harness.cpp launches them with a sequential thread
+emulation.  Inputs come from the engine's host-only synthetic generator (deterministic in its
+seed).  Outputs are written to tests/golden/*.npz and committed; the tests never need the
+reference itself.
+
+    python tests/golden/gen_golden.py
+"""
+from __future__ import annotations
+
+import ctypes as C
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+import master_thesis_gb300 as T  # noqa: E402
+import oracle as O  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+
+
+def P(a):
+    return a.ctypes.data
+
+
+def ref_settings(kind: str) -> T.Settings:
+    """'baseline': the synthetic benchmark parameters; 'reference': the reference's defaults.
+    Collision typing thresholds are lowered so that small grids exercise every collision path."""
+    s = T.baseline_settings() if kind == "baseline" else T.default_settings()
+    s.kernel.minCollisionSize = 3
+    s.kernel.collisionTypeUpdateCooldown = 2
+    return s
+
+
+def world(W, H, plates, vel, seed, kind):
+    h, ids, pl = T.generate_world(W, H, plates, vel, seed)
+    if kind == "reference":  # the reference's height scale: metres around 10000
+        h = (np.float32(10000.0) + np.float32(10000.0) * h).astype(np.float32)
+    return h, ids, pl
+
+
+def ref_step_composition(name, W, H, plates, vel, seed, kind, steps, hyd_iters, dt):
+    """`steps` steps composed of the reference's kernels in the engine's phase order, uplift
+    off and thermal off (the reference's thermal kernel is racy; see the thermal fixture)."""
+    R = O.ref()
+    st = ref_settings(kind)
+    R.ref_set_settings(C.addressof(st.kernel))
+    h, ids, pl = world(W, H, plates, vel, seed, kind)
+    N = W * H
+    w = np.zeros((H, W), np.float32)
+    s = np.zeros((H, W), np.float32)
+    f = np.zeros((H, W, 4), np.float32)
+    bm = np.zeros(T.NUM_PAIRS, np.uint8)
+    div = np.zeros(T.NUM_DIV_WORDS, np.uint32)
+    wseed = 1000
+    rec = {"h0": h.copy(), "id0": ids.copy(), "plates0": pl.copy()}
+    for it in range(steps):
+        dest = np.zeros(N, np.uint32)
+        R.ref_pixel_movements(W, H, P(ids), P(pl), P(dest))
+        word = np.zeros(N, np.uint32)
+        R.ref_register_collisions(W, H, P(ids), P(dest), P(word))
+        R.ref_collision_types(W, H, P(ids), P(h), P(word), P(pl), P(bm))
+        hn = np.zeros_like(h)
+        idn = np.zeros_like(ids)
+        acc = np.zeros_like(ids)
+        uh = np.zeros_like(h)
+        ut = np.zeros_like(ids)
+        R.ref_process_collisions(W, H, P(ids), P(h), P(word), P(pl), P(bm), P(div), wseed, it,
+                                 P(hn), P(idn), P(acc), P(uh), P(ut))
+        rc = R.ref_hydraulic(W, H, P(hn), P(w), P(s), P(f), hyd_iters, dt, wseed + it)
+        assert rc == 0
+        R.ref_accretion(W, H, P(hn), P(acc), P(idn))
+        # sub-cell centre update of applyPlateMovementChanges (plate_tectonics_kernel.cu:1871-1876)
+        cx = pl["pixelCenter_x"] + pl["direction_x"] * pl["velocity"]
+        cy = pl["pixelCenter_y"] + pl["direction_y"] * pl["velocity"]
+        pl["pixelCenter_x"] = cx - np.floor(cx)
+        pl["pixelCenter_y"] = cy - np.floor(cy)
+        h, ids = hn, idn
+        labels = np.zeros((H, W), np.uint32)
+        R.ref_ccl(W, H, P(ids), P(labels))
+        for k, v in dict(dest=dest.reshape(H, W), word=word.reshape(H, W), bitmap=bm.copy(), div=div.copy(),
+                         h=h.copy(), id=ids.copy(), acc=acc.copy(), w=w.copy(), s=s.copy(), flux=f.copy(),
+                         labels=labels, plates=pl.copy()).items():
+            rec[f"{k}_{it}"] = v
+    np.savez_compressed(OUT / f"{name}.npz", W=W, H=H, steps=steps, hyd_iters=hyd_iters, dt=np.float32(dt),
+                        seed=wseed, kind=kind, **rec)
+    print("wrote", name, "accretions", sum(int((rec[f'acc_{i}'] > 0).sum()) for i in range(steps)),
+          "typed pairs", int((bm != 0).sum()))
+
+
+def ref_thermal_isolated(name, W, H, seed):
+    """Thermal on isolated peaks (4 cells apart) with the reference's own parameters (talus
+    threshold 0.5 * 1000 m, amplitude 0.5 m): a neighbour receives at most 0.5 m and never becomes
+    active, so the reference kernel's in-place updates cannot interfere with each other and its
+    result is well defined (and equal to the gather form)."""
+    R = O.ref()
+    st = T.default_settings()
+    R.ref_set_settings(C.addressof(st.kernel))
+    rng = np.random.default_rng(seed)
+    h = np.full((H, W), np.float32(8000.0), np.float32)
+    for y in range(1, H, 4):
+        for x in range(1, W, 4):
+            if rng.random() < 0.7:
+                h[y, x] = np.float32(8000.0 + rng.uniform(300.0, 3000.0))
+            for dy in (-1, 0, 1):  # foothills: some directions of a peak fall below the talus
+                for dx in (-1, 0, 1):  # threshold; a foothill is never itself 500 m above flat land
+                    if (dy or dx) and rng.random() < 0.3:
+                        h[(y + dy) % H, (x + dx) % W] = np.float32(8000.0 + rng.uniform(0.0, 400.0))
+    out = h.copy()
+    R.ref_thermal(W, H, P(out))
+    np.savez_compressed(OUT / f"{name}.npz", W=W, H=H, h_in=h, h_out=out)
+    print("wrote", name, "changed cells", int((out != h).sum()))
+
+
+def ref_ccl_cases(name):
+    """Reference CCL labels on structured id maps that exercise wrap and diagonal links."""
+    R = O.ref()
+    cases = {}
+    rng = np.random.default_rng(5)
+    H, W = 32, 48
+    cases["random4"] = rng.integers(0, 4, (H, W)).astype(np.uint8)
+    cases["random2"] = rng.integers(0, 2, (H, W)).astype(np.uint8)
+    d = np.zeros((H, W), np.uint8)
+    for k in range(-H, W):
+        for y in range(H):
+            x = y + k
+            if 0 <= x < W and (k % 5 == 0):
+                d[y, x] = 1
+    cases["diagonals"] = d
+    a = np.zeros((H, W), np.uint8)
+    a[::3, :] = 1
+    a[:, ::7] = 2
+    cases["stripes"] = a
+    _, ids, _ = T.generate_world(W, H, 6, 1.0, 11)
+    cases["voronoi"] = ids
+    out = {}
+    for k, ids in cases.items():
+        lab = np.zeros((H, W), np.uint32)
+        R.ref_ccl(W, H, P(ids), P(lab))
+        out[f"{k}_id"] = ids
+        out[f"{k}_labels"] = lab
+    np.savez_compressed(OUT / f"{name}.npz", **out)
+    print("wrote", name)
+
+
+def main():
+    O.build(ref=True)
+    ref_step_composition("ref_steps_baseline_64x64", 64, 64, 8, 1.0, 7, "baseline", 6, 20, 0.02)
+    ref_step_composition("ref_steps_baseline_128x48", 128, 48, 5, 1.0, 3, "baseline", 6, 20, 0.02)
+    ref_step_composition("ref_steps_reference_64x64", 64, 64, 8, 1.0, 9, "reference", 6, 10, 1.0)
+    ref_thermal_isolated("ref_thermal_isolated_64x64", 64, 64, 13)
+    ref_ccl_cases("ref_ccl_cases")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,51 @@
+"""Unit properties of the oracle's building blocks (CPU)."""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+import master_thesis_gb300 as T
+import oracle as O
+
+
+def test_engine_sine_within_two_ulp_of_libm():
+    L = O.lib()
+    xs = np.concatenate([np.linspace(0.0, 10.0, 20001), np.linspace(10.0, 6.0e4, 20001),
+                         -np.linspace(0.0, 100.0, 2001)]).astype(np.float32)
+    worst = 0.0
+    for x in xs:
+        ref = np.float32(math.sin(float(x)))
+        got = np.float32(L.or_sinf(float(x)))
+        ulp = float(np.spacing(np.float32(max(abs(ref), 1e-30))))
+        worst = max(worst, abs(float(got) - float(ref)) / ulp)
+    assert worst <= 2.0, worst
+
+
+def test_lerp_endpoints_and_monotone():
+    L = O.lib()
+    assert L.or_lerp(2.0, 5.0, 0.0) == 2.0
+    assert L.or_lerp(2.0, 5.0, 1.0) == 5.0
+    vals = [L.or_lerp(-3.0, 7.0, t) for t in np.linspace(0, 1, 101)]
+    assert all(b >= a for a, b in zip(vals, vals[1:]))
+
+
+def test_gaussian_weights_normalised_symmetric():
+    w = np.zeros(7, np.float32)
+    O.lib().or_gaussian_weights(1.5, 3, w.ctypes.data)
+    assert abs(float(w.sum()) - 1.0) < 1e-6
+    np.testing.assert_array_equal(w, w[::-1])
+    assert np.all(np.diff(w[:4]) > 0)
+
+
+def test_rain_noise_range_and_determinism():
+    L = O.lib()
+    v = [L.or_rain_noise(x, y, 1234) for x in range(50) for y in range(50)]
+    assert min(v) >= -1.0 and max(v) <= 1.0
+    assert v == [L.or_rain_noise(x, y, 1234) for x in range(50) for y in range(50)]
+
+
+def test_thermal_conserves_mass_roughly():
+    h, _, _ = T.generate_world(48, 40, 6, 1.0, 4)
+    out = O.thermal(h, 10, T.baseline_settings())
+    assert abs(float(out.astype(np.float64).sum() - h.astype(np.float64).sum())) < 1e-3
