@@ -155,7 +155,8 @@ __global__ __launch_bounds__(256) void k_resolve(ResolveParams p)
     for (int i = t; i < kPlates + 1; i += 256) s_off[i] = p.off[i];
     for (int e = t; e < SY * SX; e += 256) {
         const int ly = e / SX, lx = e - ly * SX;
-        s_word[e] = p.word[cidx(x0 + lx - R, y0 + ly - R, p.W, p.H)];
+        const int gx = wrap_fast(x0 + lx - R, p.W), gy = wrap_fast(y0 + ly - R, p.H);
+        s_word[e] = p.word[(size_t)gy * p.W + gx];
     }
     __syncthreads();
     if (R > 0) {

@@ -126,9 +126,20 @@ __host__ __device__ __forceinline__ int wrapc(int c, int n)
     return r + (n & (r >> 31));
 }
 
+// Same result as wrapc; coordinates within one period of the grid (c in [-n, 2n), the case of
+// every stencil halo and plate displacement) wrap without an integer division.
+__host__ __device__ __forceinline__ int wrap_fast(int c, int n)
+{
+    if ((unsigned)(c + n) < 3u * (unsigned)n) {
+        c = c < 0 ? c + n : c;
+        return c >= n ? c - n : c;
+    }
+    return wrapc(c, n);
+}
+
 __host__ __device__ __forceinline__ uint32_t cidx(int x, int y, int W, int H)
 {
-    return (uint32_t)(wrapc(y, H) * W + wrapc(x, W));
+    return (uint32_t)(wrap_fast(y, H) * W + wrap_fast(x, W));
 }
 
 // upperTriangleIndexUnchecked(i, j, 255), i < j (src/cuda_compute/cuda_helper.cuh:97-104)
