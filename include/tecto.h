@@ -260,6 +260,28 @@ int tecto_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t 
                      uint32_t *vals_out, size_t n, int key_bits, void *scratch,
                      size_t scratch_bytes, tecto_stream_t stream);
 
+/* The same stable sort for callers that cannot allocate device memory: it needs no scratch
+ * argument and makes no allocation of any kind (no cudaMalloc, cudaFree or allocating library
+ * call).  This entry point has no counterpart in the reference.  Who needs it: a host that hands
+ * the engine a fixed memory budget and owns every allocation (a plugin inside a renderer or game
+ * engine), and a per-frame loop such as the reference's GUI loop, where cudaFree's implicit device
+ * synchronisation would stall the frame.
+ *
+ * Its scratch is one fixed array in device memory, TECTO_SORT_NOALLOC_MAX_PAIRS pairs large
+ * (9.4 MB), which every GPU that loads the library holds until the process exits.  Limits
+ * and rules:
+ *  - n > TECTO_SORT_NOALLOC_MAX_PAIRS is rejected with TECTO_ERR_INVALID (nothing runs);
+ *  - outputs must not alias the inputs (TECTO_ERR_INVALID);
+ *  - the first call on each device resolves the array's device address with that device current;
+ *    make that first call before any stream capture;
+ *  - all calls share the one array: two calls whose work overlaps on the GPU (different streams,
+ *    or different host threads on the same device) race and corrupt each other's results, so
+ *    serialise them.  Each call clears the parts that must start at zero itself.
+ * Synchronous: returns after the result is in keys_out/vals_out. */
+#define TECTO_SORT_NOALLOC_MAX_PAIRS ((size_t)1 << 20)
+int tecto_sort_pairs_noalloc(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_out,
+                             uint32_t *vals_out, size_t n, int key_bits, tecto_stream_t stream);
+
 /* ---- status -------------------------------------------------------------------------- */
 
 /* Number of engine kernels enqueued for this world so far (graph replays count the kernels of the

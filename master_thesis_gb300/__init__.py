@@ -183,6 +183,7 @@ def _declare(L: C.CDLL) -> None:
         "tecto_phase_ccl": ([P, C.c_int, P], C.c_int),
         "tecto_sort_scratch_bytes": ([C.c_size_t, C.c_int], C.c_size_t),
         "tecto_sort_pairs": ([P, P, P, P, C.c_size_t, C.c_int, P, C.c_size_t, P], C.c_int),
+        "tecto_sort_pairs_noalloc": ([P, P, P, P, C.c_size_t, C.c_int, P], C.c_int),
         "tecto_world_check": ([P, P], C.c_int),
         "tecto_world_launch_count": ([P, C.POINTER(C.c_uint64)], C.c_int),
         "tecto_last_error_string": ([], C.c_char_p),

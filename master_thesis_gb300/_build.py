@@ -20,6 +20,7 @@ LIB = PKG / "libtecto.so"
 SOURCES = [
     "tecto_api.cu",
     "k_sort.cu",
+    "k_sort_noalloc.cu",
     "k_collide.cu",
     "k_resolve.cu",
     "k_erosion.cu",
