@@ -127,7 +127,9 @@ typedef struct tecto_step_settings {
     int upliftRadius;         /* taps on each side (<= 8) */
     int cclConnectivity;      /* TECTO_CCL_* */
     int sortRadixBits;        /* 0 = autotuned; else 6..8 */
-    int reserved[7];
+    int hydraulicTile;        /* 0 = default; 1: 64x16/256 threads, 2: 64x32/256, 3: 64x32/512,
+                                 4: 64x32/1024, 5: 64x64/1024 */
+    int reserved[6];
 } tecto_step_settings;
 
 typedef struct tecto_settings {

@@ -117,7 +117,8 @@ class StepSettings(C.Structure):
         ("upliftRadius", C.c_int),
         ("cclConnectivity", C.c_int),
         ("sortRadixBits", C.c_int),
-        ("reserved", C.c_int * 7),
+        ("hydraulicTile", C.c_int),
+        ("reserved", C.c_int * 6),
     ]
 
 

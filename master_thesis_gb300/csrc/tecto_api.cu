@@ -179,6 +179,7 @@ int tecto_world_create(const tecto_settings *settings, int width, int height, ui
     const size_t o_k0 = L.add(N * 4), o_k1 = L.add(N * 4);
     const size_t o_v0 = L.add(N * 4), o_v1 = L.add(N * 4);
     const size_t o_lab = L.add(N * 4);
+    const size_t o_rain = L.add(N * 4);
     const size_t o_vel = L.add(N * 8);
     const size_t o_s1b = L.add(N * 4);
     const size_t o_acc = L.add(N * 8);
@@ -216,6 +217,7 @@ int tecto_world_create(const tecto_settings *settings, int width, int height, ui
     b.vals[0] = (uint32_t *)(base + o_v0);
     b.vals[1] = (uint32_t *)(base + o_v1);
     b.labels = (uint32_t *)(base + o_lab);
+    b.rain = (float *)(base + o_rain);
     b.vel = (float2 *)(base + o_vel);
     b.s1 = (float *)(base + o_s1b);
     b.acc = (unsigned long long *)(base + o_acc);

@@ -68,6 +68,7 @@ struct WorldBuffers {
     uint32_t *keys[2];      // sort ping-pong
     uint32_t *vals[2];
     uint32_t *labels;       // CCL labels
+    float *rain;            // this step's rain increment per cell (constant over sub-iterations)
     float2 *vel;            // water velocity, split hydraulic path only
     float *s1;              // sediment before transport, split hydraulic path only
     unsigned long long *acc;  // accretion marks: ((dest + 1) << 8) | (255 - owner), atomicMax

@@ -495,15 +495,22 @@ void or_thermal(int W, int H, float *h, int iters, const tecto_kernel_settings *
                 const size_t i = (size_t)y * W + x;
                 const float hc = h[i];
                 float v = hc;
+                /* a flow that evaluates to exactly zero moves nothing and is skipped */
                 if (tot[i] > 0.0f)
                     for (int d = 0; d < 8; ++d) {
                         const float diff = hc - h[cidx(x + TH_DX[d], y + TH_DY[d], W, H)];
-                        if (diff > thr) v = v - (A * (diff / tot[i])) * S;
+                        if (diff > thr) {
+                            const float f = (A * (diff / tot[i])) * S;
+                            if (f != 0.0f) v = v - f;
+                        }
                     }
                 for (int d = 0; d < 8; ++d) {
                     const uint32_t nb = cidx(x + TH_DX[d], y + TH_DY[d], W, H);
                     const float diff = h[nb] - hc;
-                    if (diff > thr && tot[nb] > 0.0f) v = v + (A * (diff / tot[nb])) * S;
+                    if (diff > thr && tot[nb] > 0.0f) {
+                        const float f = (A * (diff / tot[nb])) * S;
+                        if (f != 0.0f) v = v + f;
+                    }
                 }
                 hn[i] = v;
             }

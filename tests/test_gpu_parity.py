@@ -113,6 +113,31 @@ def test_phases_match_oracle(kind, W, H):
     print(kind, W, H, {k: max(v) for k, v in report.items()})
 
 
+@pytest.mark.parametrize("tile", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("W,H,dt", [(100, 60, 0.02), (33, 17, 0.02), (300, 200, 0.02), (128, 96, 1.0)])
+def test_hydraulic_tile_variants_match_oracle(tile, W, H, dt):
+    """Every hydraulic tile shape (interior tiles without wrap, edge tiles with it) gives the
+    oracle's result; dt 1.0 takes the split transport path."""
+    st, w = make_world("baseline", W, H)
+    st.step.hydraulicTile = tile
+    w.set_settings(st)
+    rng = np.random.default_rng(W * H + tile)
+    water = np.abs(rng.normal(0, 0.2, (H, W))).astype(np.float32)
+    sed = np.abs(rng.normal(0, 0.05, (H, W))).astype(np.float32)
+    flux = np.abs(rng.normal(0, 0.02, (H, W, 4))).astype(np.float32)
+    w.upload(T.FIELD_WATER, water)
+    w.upload(T.FIELD_SEDIMENT, sed)
+    w.upload(T.FIELD_FLUX, flux)
+    h = w.download(T.FIELD_HEIGHT)
+    w.hydraulic(7, dt)
+    hh, ww, ss, ff = O.hydraulic(h, water, sed, flux, 7, dt, 1000, st)
+    report = {}
+    for name, f, want in (("h", T.FIELD_HEIGHT, hh), ("w", T.FIELD_WATER, ww), ("s", T.FIELD_SEDIMENT, ss),
+                          ("flux", T.FIELD_FLUX, ff)):
+        assert_fp(name, w.download(f), want, 0, report)
+    w.check()
+
+
 @pytest.mark.parametrize("W,H,steps", [(64, 64, 12), (100, 60, 12), (256, 256, 6)])
 def test_graph_steps_match_oracle(torch_stream, W, H, steps):
     st, w = make_world("baseline", W, H)
