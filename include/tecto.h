@@ -284,6 +284,80 @@ int tecto_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t 
 int tecto_sort_pairs_noalloc(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_out,
                              uint32_t *vals_out, size_t n, int key_bits, tecto_stream_t stream);
 
+/* ---- batches: many worlds, one launch per phase ----------------------------------------
+ *
+ * The reference steps one world at a time; it has no counterpart for these calls.  A batch
+ * advances all its worlds together: every phase is one kernel launch over a work list of
+ * (world, tile) items, the sort runs once over all the batch's cells, and a step is replayed as
+ * one CUDA graph.  Worlds keep their own device state and keep it between steps; results are
+ * identical to stepping each world alone.  All worlds of a batch share one settings struct and one
+ * device.  While a world is in a batch, tecto_world_step and the phase calls refuse it. */
+typedef struct tecto_batch tecto_batch;
+int tecto_batch_create(tecto_batch **out);
+int tecto_batch_destroy(tecto_batch *batch);  /* worlds stay alive and leave the batch */
+int tecto_batch_add(tecto_batch *batch, tecto_world *world, tecto_stream_t stream);
+int tecto_batch_remove(tecto_batch *batch, tecto_world *world);
+int tecto_batch_step(tecto_batch *batch, int nSteps, tecto_stream_t stream);
+int tecto_batch_size(const tecto_batch *batch, int *worlds, size_t *cells);
+int tecto_batch_launch_count(const tecto_batch *batch, uint64_t *count);
+int tecto_batch_check(tecto_batch *batch, tecto_stream_t stream);
+
+/* Device bytes one world of width x height holds, including its share of batch buffers: the
+ * admission cost used by the server below. */
+size_t tecto_world_bytes(int width, int height);
+
+/* ---- serving: continuous batching of world-generation requests -------------------------
+ *
+ * No counterpart in the reference (it runs one interactive world).  A request asks for a world of
+ * width x height with `plates` plates (synthetic generator, seeds gen_seed / world_seed) to be
+ * advanced `steps` steps.  The server keeps every admitted world resident in HBM, advances all of
+ * them one step per tick as one batch, admits waiting requests first-come first-served whenever
+ * their tecto_world_bytes fit the budget (and fewer than max_worlds are active), and retires
+ * finished worlds at once, so new requests join while others are mid-flight.  A request larger
+ * than the whole budget is rejected (TECTO_ERR_BUDGET). */
+typedef struct tecto_server tecto_server;
+typedef struct tecto_request {
+    int width, height, plates, steps;
+    float velRange;
+    uint64_t genSeed;
+    uint32_t worldSeed;
+    double arrival_s;     /* arrival time, seconds from the start of a trace */
+} tecto_request;
+typedef struct tecto_request_result {
+    int status;           /* TECTO_OK, TECTO_ERR_BUDGET (rejected) or another error */
+    double arrival_s, admit_s, finish_s;
+    float height_checksum; /* sum of the final height field (float64 accumulated, then rounded) */
+} tecto_request_result;
+typedef struct tecto_server_stats {
+    int completed, rejected, ticks, max_active;
+    double wall_s;                 /* trace start to last completion */
+    double cell_updates;           /* sum over completed requests of cells x steps */
+    double cell_updates_per_s;
+    double latency_p50_s, latency_p99_s, latency_mean_s;
+    double peak_bytes;             /* largest admitted footprint */
+} tecto_server_stats;
+
+#define TECTO_SERVER_DRY_RUN 1     /* flag: no device work; a tick costs `dry_tick_s_per_mcell` */
+
+int tecto_server_create(const tecto_settings *settings, size_t budget_bytes, int max_worlds, int flags,
+                        tecto_server **out);
+int tecto_server_destroy(tecto_server *server);
+/* Replay a trace in real time with continuous batching; results[i] belongs to requests[i]. */
+int tecto_server_run_trace(tecto_server *server, const tecto_request *requests, int n,
+                           tecto_stream_t stream, tecto_request_result *results,
+                           tecto_server_stats *stats);
+/* The same trace served one request at a time with the plain one-world path (the baseline). */
+int tecto_server_run_trace_sequential(tecto_server *server, const tecto_request *requests, int n,
+                                      tecto_stream_t stream, tecto_request_result *results,
+                                      tecto_server_stats *stats);
+/* Dry-run cost model: seconds one tick takes per million active cells (default 2e-4). */
+int tecto_server_set_dry_cost(tecto_server *server, double seconds_per_mcell_step);
+
+/* Device-side synthetic generator: same result as tecto_generate_world_host, computed on the GPU
+ * (the on-device world init the server uses). */
+int tecto_world_init_synthetic_device(tecto_world *world, int numPlates, float velRange,
+                                      uint64_t genSeed, tecto_stream_t stream);
+
 /* ---- status -------------------------------------------------------------------------- */
 
 /* Number of engine kernels enqueued for this world so far (graph replays count the kernels of the

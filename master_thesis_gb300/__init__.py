@@ -141,6 +141,36 @@ class Plate(C.Structure):
     ]
 
 
+class Request(C.Structure):
+    """tecto_request: one world-generation job for the server."""
+    _fields_ = [
+        ("width", C.c_int), ("height", C.c_int), ("plates", C.c_int), ("steps", C.c_int),
+        ("velRange", C.c_float), ("genSeed", C.c_uint64), ("worldSeed", C.c_uint32),
+        ("arrival_s", C.c_double),
+    ]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [
+        ("status", C.c_int), ("arrival_s", C.c_double), ("admit_s", C.c_double), ("finish_s", C.c_double),
+        ("height_checksum", C.c_float),
+    ]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [
+        ("completed", C.c_int), ("rejected", C.c_int), ("ticks", C.c_int), ("max_active", C.c_int),
+        ("wall_s", C.c_double), ("cell_updates", C.c_double), ("cell_updates_per_s", C.c_double),
+        ("latency_p50_s", C.c_double), ("latency_p99_s", C.c_double), ("latency_mean_s", C.c_double),
+        ("peak_bytes", C.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+SERVER_DRY_RUN = 1
+
 PLATE_DTYPE = np.dtype(
     [("velocity", "<f4"), ("direction_x", "<f4"), ("direction_y", "<f4"),
      ("pixelCenter_x", "<f4"), ("pixelCenter_y", "<f4")]
@@ -187,6 +217,23 @@ def _declare(L: C.CDLL) -> None:
         "tecto_sort_pairs_noalloc": ([P, P, P, P, C.c_size_t, C.c_int, P], C.c_int),
         "tecto_world_check": ([P, P], C.c_int),
         "tecto_world_launch_count": ([P, C.POINTER(C.c_uint64)], C.c_int),
+        "tecto_world_bytes": ([C.c_int, C.c_int], C.c_size_t),
+        "tecto_world_init_synthetic_device": ([P, C.c_int, C.c_float, C.c_uint64, P], C.c_int),
+        "tecto_batch_create": ([C.POINTER(P)], C.c_int),
+        "tecto_batch_destroy": ([P], C.c_int),
+        "tecto_batch_add": ([P, P, P], C.c_int),
+        "tecto_batch_remove": ([P, P], C.c_int),
+        "tecto_batch_step": ([P, C.c_int, P], C.c_int),
+        "tecto_batch_size": ([P, C.POINTER(C.c_int), C.POINTER(C.c_size_t)], C.c_int),
+        "tecto_batch_launch_count": ([P, C.POINTER(C.c_uint64)], C.c_int),
+        "tecto_batch_check": ([P, P], C.c_int),
+        "tecto_server_create": ([C.POINTER(Settings), C.c_size_t, C.c_int, C.c_int, C.POINTER(P)], C.c_int),
+        "tecto_server_destroy": ([P], C.c_int),
+        "tecto_server_run_trace": ([P, C.POINTER(Request), C.c_int, P, C.POINTER(RequestResult),
+                                    C.POINTER(ServerStats)], C.c_int),
+        "tecto_server_run_trace_sequential": ([P, C.POINTER(Request), C.c_int, P, C.POINTER(RequestResult),
+                                               C.POINTER(ServerStats)], C.c_int),
+        "tecto_server_set_dry_cost": ([P, C.c_double], C.c_int),
         "tecto_last_error_string": ([], C.c_char_p),
         "tecto_version": ([], C.c_char_p),
     }
@@ -361,6 +408,102 @@ class World:
 
     def check(self, stream=None):
         check(lib().tecto_world_check(self.ptr, _stream(stream)), "tecto_world_check")
+
+
+def _world_init_device(self, plates: int, vel_range: float, gen_seed: int, stream=None) -> None:
+    check(lib().tecto_world_init_synthetic_device(self.ptr, plates, vel_range, gen_seed, _stream(stream)),
+          "tecto_world_init_synthetic_device")
+
+
+World.init_synthetic_device = _world_init_device
+
+
+def world_bytes(W: int, H: int) -> int:
+    return int(lib().tecto_world_bytes(W, H))
+
+
+class Batch:
+    """Many worlds advanced together, one kernel launch per phase (tecto_batch)."""
+
+    def __init__(self):
+        p = C.c_void_p()
+        check(lib().tecto_batch_create(C.byref(p)), "tecto_batch_create")
+        self.ptr = p
+        self.worlds: list[World] = []
+
+    def add(self, world: World, stream=None) -> None:
+        check(lib().tecto_batch_add(self.ptr, world.ptr, _stream(stream)), "tecto_batch_add")
+        self.worlds.append(world)
+
+    def remove(self, world: World) -> None:
+        check(lib().tecto_batch_remove(self.ptr, world.ptr), "tecto_batch_remove")
+        self.worlds.remove(world)
+
+    def step(self, n: int = 1, stream=None) -> None:
+        check(lib().tecto_batch_step(self.ptr, n, _stream(stream)), "tecto_batch_step")
+
+    def size(self) -> tuple[int, int]:
+        nw, nc = C.c_int(), C.c_size_t()
+        check(lib().tecto_batch_size(self.ptr, C.byref(nw), C.byref(nc)), "tecto_batch_size")
+        return nw.value, nc.value
+
+    @property
+    def launches(self) -> int:
+        v = C.c_uint64()
+        check(lib().tecto_batch_launch_count(self.ptr, C.byref(v)), "tecto_batch_launch_count")
+        return v.value
+
+    def check(self, stream=None) -> None:
+        check(lib().tecto_batch_check(self.ptr, _stream(stream)), "tecto_batch_check")
+
+    def close(self) -> None:
+        if getattr(self, "ptr", None):
+            lib().tecto_batch_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Continuous-batching server for world-generation requests (tecto_server)."""
+
+    def __init__(self, settings: Settings, budget_bytes: int, max_worlds: int = 0, dry_run: bool = False):
+        p = C.c_void_p()
+        check(lib().tecto_server_create(C.byref(settings), budget_bytes, max_worlds,
+                                        SERVER_DRY_RUN if dry_run else 0, C.byref(p)), "tecto_server_create")
+        self.ptr = p
+
+    def set_dry_cost(self, seconds_per_mcell_step: float) -> None:
+        check(lib().tecto_server_set_dry_cost(self.ptr, seconds_per_mcell_step), "tecto_server_set_dry_cost")
+
+    def _run(self, fn, requests, stream):
+        n = len(requests)
+        reqs = (Request * max(n, 1))(*requests)
+        res = (RequestResult * max(n, 1))()
+        st = ServerStats()
+        check(fn(self.ptr, reqs, n, _stream(stream), res, C.byref(st)), fn.__name__)
+        return list(res)[:n], st
+
+    def run_trace(self, requests, stream=None):
+        return self._run(lib().tecto_server_run_trace, requests, stream)
+
+    def run_trace_sequential(self, requests, stream=None):
+        return self._run(lib().tecto_server_run_trace_sequential, requests, stream)
+
+    def close(self) -> None:
+        if getattr(self, "ptr", None):
+            lib().tecto_server_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def load_config(path: str | os.PathLike) -> tuple[Settings, int, int]:

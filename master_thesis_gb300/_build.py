@@ -19,6 +19,8 @@ LIB = PKG / "libtecto.so"
 
 SOURCES = [
     "tecto_api.cu",
+    "tecto_batch.cu",
+    "tecto_server.cu",
     "k_sort.cu",
     "k_sort_noalloc.cu",
     "k_collide.cu",

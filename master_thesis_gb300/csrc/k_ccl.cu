@@ -90,11 +90,29 @@ __device__ __forceinline__ void g_union(uint32_t *L, uint32_t a, uint32_t b)
     }
 }
 
-__global__ __launch_bounds__(256) void k_ccl_local(const uint8_t *id, uint32_t *labels, int W, int H,
-                                                   int mode)
+// The world of this block's tile, or nullptr when the world's labelling is not due this step.
+__device__ __forceinline__ const WorldDev *ccl_tile(const WorldDev *worlds, const uint2 *tiles, int period,
+                                                    int *x0, int *y0)
+{
+    int wi, tx, ty;
+    tile_of(tiles[blockIdx.x], &wi, &tx, &ty);
+    const WorldDev *wd = worlds + wi;
+    if (period > 0 && wd->ctl->iteration % (uint32_t)period != 0u) return nullptr;
+    *x0 = tx * CX;
+    *y0 = ty * CY;
+    return wd;
+}
+
+__global__ __launch_bounds__(256) void k_ccl_local(const WorldDev *worlds, const uint2 *tiles, int cur_id,
+                                                   int mode, int period)
 {
     __shared__ int par[CX * CY];
-    const int x0 = blockIdx.x * CX, y0 = blockIdx.y * CY;
+    int x0, y0;
+    const WorldDev *wd = ccl_tile(worlds, tiles, period, &x0, &y0);
+    if (!wd) return;
+    const uint8_t *id = wd->id[cur_id];
+    uint32_t *labels = wd->labels;
+    const int W = wd->W, H = wd->H;
     const int tw = min(CX, W - x0), th = min(CY, H - y0);
     for (int e = threadIdx.x; e < CX * CY; e += blockDim.x) par[e] = e;
     __syncthreads();
@@ -124,10 +142,15 @@ __global__ __launch_bounds__(256) void k_ccl_local(const uint8_t *id, uint32_t *
 
 // Unions across tile borders: only cells on a tile's top row or left/right column have edges
 // leaving the tile.
-__global__ __launch_bounds__(128) void k_ccl_border(const uint8_t *id, uint32_t *labels, int W, int H,
-                                                    int mode)
+__global__ __launch_bounds__(128) void k_ccl_border(const WorldDev *worlds, const uint2 *tiles, int cur_id,
+                                                    int mode, int period)
 {
-    const int x0 = blockIdx.x * CX, y0 = blockIdx.y * CY;
+    int x0, y0;
+    const WorldDev *wd = ccl_tile(worlds, tiles, period, &x0, &y0);
+    if (!wd) return;
+    const uint8_t *id = wd->id[cur_id];
+    uint32_t *labels = wd->labels;
+    const int W = wd->W, H = wd->H;
     const int tw = min(CX, W - x0), th = min(CY, H - y0);
     const int nb = tw + 2 * th;  // top row, left column, right column (corners repeat harmlessly)
     const int dxs[4] = {-1, 0, -1, 1}, dys[4] = {0, -1, -1, -1};
@@ -148,28 +171,39 @@ __global__ __launch_bounds__(128) void k_ccl_border(const uint8_t *id, uint32_t 
     }
 }
 
-__global__ void k_ccl_flatten(uint32_t *labels, uint32_t n)
+__global__ void k_ccl_flatten(const WorldDev *worlds, const uint2 *tiles, int period)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) labels[i] = g_find(labels, i);
+    int x0, y0;
+    const WorldDev *wd = ccl_tile(worlds, tiles, period, &x0, &y0);
+    if (!wd) return;
+    uint32_t *labels = wd->labels;
+    const int W = wd->W, H = wd->H;
+    for (int e = threadIdx.x; e < CX * CY; e += blockDim.x) {
+        const int ly = e / CX, lx = e - ly * CX;
+        const int x = x0 + lx, y = y0 + ly;
+        if (x < W && y < H) {
+            const uint32_t i = (uint32_t)y * (uint32_t)W + (uint32_t)x;
+            labels[i] = g_find(labels, i);
+        }
+    }
 }
 
 }  // namespace
 
-int launch_ccl(tecto_world *w, int connectivity, cudaStream_t st)
+int launch_ccl(Batch &b, int connectivity, bool due_only, cudaStream_t st)
 {
     if (connectivity != TECTO_CCL_4 && connectivity != TECTO_CCL_8 && connectivity != TECTO_CCL_REF8) {
         set_error("cclConnectivity must be 4, 8 or 9 (ref8)");
         return TECTO_ERR_INVALID;
     }
-    const dim3 grid((unsigned)((w->W + CX - 1) / CX), (unsigned)((w->H + CY - 1) / CY));
-    const uint8_t *id = w->b.id[w->cur_id];
-    k_ccl_local<<<grid, 256, 0, st>>>(id, w->b.labels, w->W, w->H, connectivity);
-    k_ccl_border<<<grid, 128, 0, st>>>(id, w->b.labels, w->W, w->H, connectivity);
-    const uint32_t n = (uint32_t)w->N;
-    k_ccl_flatten<<<(n + 255) / 256, 256, 0, st>>>(w->b.labels, n);
+    const int period = due_only ? (b.settings.sim.iterationsForCCL > 0 ? b.settings.sim.iterationsForCCL : 1) : 0;
+    const unsigned grid = (unsigned)b.ntiles[TK_CCL];
+    const uint2 *tiles = b.d_tiles[TK_CCL];
+    k_ccl_local<<<grid, 256, 0, st>>>(b.d_worlds, tiles, b.cur_id, connectivity, period);
+    k_ccl_border<<<grid, 128, 0, st>>>(b.d_worlds, tiles, b.cur_id, connectivity, period);
+    k_ccl_flatten<<<grid, 256, 0, st>>>(b.d_worlds, tiles, period);
     TECTO_CUDA(cudaGetLastError());
-    w->launches += 3;
+    b.launches += 3;
     return TECTO_OK;
 }
 

@@ -7,25 +7,27 @@ namespace tecto {
 namespace {
 
 // Per-plate integer displacement (getPixelMovements, :248-257) and the sub-cell centre update
-// of applyPlateMovementChanges (:1871-1878).  Also resets the per-step counters.
-__global__ void k_plates(tecto_plate *plates, int2 *off, Control *ctl)
+// of applyPlateMovementChanges (:1871-1878), one block per world.  Also resets the world's
+// per-step accretion list.
+__global__ void k_plates(const WorldDev *worlds)
 {
+    const WorldDev &wd = worlds[blockIdx.x];
     const int k = threadIdx.x;
     if (k < kPlates) {
-        tecto_plate p = plates[k];
+        tecto_plate p = wd.plates[k];
         const float mx = p.direction_x * p.velocity;
         const float my = p.direction_y * p.velocity;
         const float cx = p.pixelCenter_x + mx;
         const float cy = p.pixelCenter_y + my;
         const float fx = floorf(cx), fy = floorf(cy);
-        off[k] = make_int2((int)fx, (int)fy);
+        wd.off[k] = make_int2((int)fx, (int)fy);
         p.pixelCenter_x = cx - fx;
         p.pixelCenter_y = cy - fy;
-        plates[k] = p;
+        wd.plates[k] = p;
     } else if (k == kPlates) {
-        off[k] = make_int2(0, 0);
+        wd.off[k] = make_int2(0, 0);
     }
-    if (k == 0) ctl->acc_count = 0;
+    if (k == 0) wd.ctl->acc_count = 0;
 }
 
 // writeCollision's classification (:794-836): returns category 0..4 or -1 to skip.  The early
@@ -48,44 +50,58 @@ __device__ __forceinline__ int evidence_category(const uint8_t *bm, uint8_t A, u
     return 3;
 }
 
-// Segmented winner pick over the sorted (destination, source) pairs: the first position of
-// each destination's run builds the packed arrival word of registerPlateCollisions (:273-298)
-// from its first four sources (ascending source order), writes zero words into the gap of
-// destinations nobody moved into, and for convergent cells adds the collision-type evidence of
-// the determineCollisionType kernel (:838-888) with warp-aggregated atomics.
+// Segmented winner pick over the sorted (destination, source) pairs of the whole batch: the
+// first position of each destination's run builds the packed arrival word of
+// registerPlateCollisions (:273-298) from its first four sources (ascending source order),
+// writes zero words into the gap of destinations nobody moved into, and for convergent cells
+// adds the collision-type evidence of the determineCollisionType kernel (:838-888) with
+// warp-aggregated atomics.
 __global__ __launch_bounds__(256) void k_words(const uint32_t *keys, const uint32_t *vals, uint32_t n,
-                                               uint32_t N, const uint8_t *id_old, const float *h_old,
-                                               const uint8_t *bm, PairCounts *counts, uint32_t *word,
-                                               float thr, int cooldown)
+                                               const WorldDev *worlds, const uint32_t *vbase, int nworlds,
+                                               int cur_id, int cur_h, float thr, int cooldown)
 {
+    __shared__ uint32_t s_vbase[kMaxBatchWorlds + 1];
+    for (int i = threadIdx.x; i <= nworlds; i += blockDim.x) s_vbase[i] = vbase[i];
+    __syncthreads();
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     const unsigned lane = threadIdx.x & 31u;
     const bool valid = j < n;
-    uint32_t key = 0;
     bool leader = false;
     uint8_t ids[4] = {0, 0, 0, 0};
     float hs[4] = {0, 0, 0, 0};
     int cnt = 0;
+    int wi = 0;
     if (valid) {
-        key = keys[j];
+        const uint32_t key = keys[j];
         const uint32_t prev = j > 0 ? keys[j - 1] : 0xffffffffu;
         leader = j == 0 || prev != key;
         if (leader) {
+            // gap of destinations without arrivals (they may belong to earlier worlds)
             const uint32_t gap0 = j == 0 ? 0u : prev + 1u;
-            for (uint32_t c = gap0; c < key; ++c) word[c] = 0u;
+            for (uint32_t c = gap0; c < key; ++c) {
+                const WorldDev &gw = worlds[find_world(s_vbase, nworlds, c)];
+                gw.word[c - gw.vbase] = 0u;
+            }
+            wi = find_world(s_vbase, nworlds, key);
+            const WorldDev &wd = worlds[wi];
             uint32_t wv = 0;
             for (int k = 0; k < 4; ++k) {
                 if (j + k >= n || keys[j + k] != key) break;
-                const uint32_t src = vals[j + k];
-                ids[k] = id_old[src];
-                hs[k] = h_old[src];  // determineCollisionHeight: height at the arrival's source
+                const uint32_t src = vals[j + k] - wd.vbase;
+                ids[k] = wd.id[cur_id][src];
+                hs[k] = wd.h[cur_h][src];  // determineCollisionHeight: height at the arrival's source
                 wv |= (uint32_t)(255u - ids[k]) << (8 * k);
                 ++cnt;
             }
-            word[key] = wv;
+            wd.word[key - wd.vbase] = wv;
         }
-        if (j == n - 1)
-            for (uint32_t c = key + 1u; c < N; ++c) word[c] = 0u;
+        if (j == n - 1) {
+            const uint32_t total = s_vbase[nworlds];  // vbase[n] holds the batch's cell count
+            for (uint32_t c = key + 1u; c < total; ++c) {
+                const WorldDev &gw = worlds[find_world(s_vbase, nworlds, c)];
+                gw.word[c - gw.vbase] = 0u;
+            }
+        }
     }
     // pairs in determineCollisionType's order for 2, 3 and 4 arrivals (counts are sums, so the
     // order only has to cover the same pairs)
@@ -94,6 +110,7 @@ __global__ __launch_bounds__(256) void k_words(const uint32_t *keys, const uint3
     const uint8_t PB[6] = {1, 2, 3, 2, 3, 3};
     const uint8_t PA3[3] = {0, 0, 1};
     const uint8_t PB3[3] = {1, 2, 2};
+    const uint8_t *bm = npairs ? worlds[wi].type_bitmap : nullptr;
 #pragma unroll
     for (int slot = 0; slot < 6; ++slot) {
         uint32_t keyv = 0xffffffffu;
@@ -103,21 +120,25 @@ __global__ __launch_bounds__(256) void k_words(const uint32_t *keys, const uint3
             const int a = cnt == 3 ? PA3[slot] : PA[slot];
             const int b = cnt == 3 ? PB3[slot] : PB[slot];
             cat = evidence_category(bm, ids[a], ids[b], hs[a], hs[b], thr, cooldown, &pair);
-            if (cat >= 0) keyv = pair * 5u + (uint32_t)cat;
+            // aggregation key: world, pair and category (worlds differ within a warp rarely)
+            if (cat >= 0) keyv = ((uint32_t)wi * (uint32_t)kPairs + pair) * 5u + (uint32_t)cat;
         }
         const unsigned any = __ballot_sync(0xffffffffu, keyv != 0xffffffffu);
         if (any == 0) continue;
         const unsigned peers = __match_any_sync(0xffffffffu, keyv);
         if (keyv != 0xffffffffu && (peers & ((1u << lane) - 1u)) == 0)
-            atomicAdd(&counts[pair].c[cat], __popc(peers));
+            atomicAdd(&worlds[wi].counts[pair].c[cat], __popc(peers));
     }
 }
 
-// createCollisionTypeMatrix (:890-972).  Also clears the evidence for the next step.
-__global__ void k_type_matrix(PairCounts *counts, uint8_t *bm, int cooldown, int minSize)
+// createCollisionTypeMatrix (:890-972) for every world of the batch; also clears the evidence.
+__global__ void k_type_matrix(const WorldDev *worlds, int cooldown, int minSize)
 {
     const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (uint32_t)kPairs) return;
+    const WorldDev &wd = worlds[blockIdx.y];
+    PairCounts *counts = wd.counts;
+    uint8_t *bm = wd.type_bitmap;
     const PairCounts pc = counts[idx];
     int *cp = counts[idx].c;
     cp[0] = cp[1] = cp[2] = cp[3] = cp[4] = 0;
@@ -145,58 +166,56 @@ __global__ void k_type_matrix(PairCounts *counts, uint8_t *bm, int cooldown, int
 
 }  // namespace
 
-int launch_plates(tecto_world *w, cudaStream_t st)
+int launch_plates(Batch &b, cudaStream_t st)
 {
-    const int rc = launch_clear_marks(w, st);  // must run before k_plates resets the list count
+    const int rc = launch_clear_marks(b, st);  // must run before k_plates resets the list count
     if (rc != TECTO_OK) return rc;
-    k_plates<<<1, 256, 0, st>>>(w->b.plates, w->b.off, w->b.ctl);
+    k_plates<<<(unsigned)b.members.size(), 256, 0, st>>>(b.d_worlds);
     TECTO_CUDA(cudaGetLastError());
-    w->launches += 1;
+    b.launches += 1;
     return TECTO_OK;
 }
 
-int launch_sort_keys(tecto_world *w, cudaStream_t st)
+int launch_sort_keys(Batch &b, cudaStream_t st)
 {
     SortArgs a{};
-    a.gen_id = w->b.id[w->cur_id];
-    a.gen_off = w->b.off;
-    a.W = w->W;
-    a.H = w->H;
-    a.keys[0] = w->b.keys[0];
-    a.keys[1] = w->b.keys[1];
-    a.vals[0] = w->b.vals[0];
-    a.vals[1] = w->b.vals[1];
-    a.n = w->N;
-    a.key_bits = key_bits_for(w->N);
+    a.worlds = b.d_worlds;
+    a.vbase = b.d_vbase;
+    a.nworlds = (int)b.members.size();
+    a.cur_id = b.cur_id;
+    a.keys[0] = b.keys[0];
+    a.keys[1] = b.keys[1];
+    a.vals[0] = b.vals[0];
+    a.vals[1] = b.vals[1];
+    a.n = b.total;
+    a.key_bits = key_bits_for(b.total);
     int half = 0;
-    const int rc = run_sort(a, w->b.sort, st, &half);
+    const int rc = run_sort(a, b.sort, st, &half);
     if (rc != TECTO_OK) return rc;
-    w->sort_final = half;
-    w->launches += 2 + (uint64_t)sort_passes_for(a.key_bits);
+    b.sort_final = half;
+    b.launches += 2 + (uint64_t)sort_passes_for(a.key_bits);
     return TECTO_OK;
 }
 
-int launch_words(tecto_world *w, cudaStream_t st)
+int launch_words(Batch &b, cudaStream_t st)
 {
-    const uint32_t n = (uint32_t)w->N;
-    const tecto_kernel_settings &ks = w->settings.kernel;
-    k_words<<<(n + 255) / 256, 256, 0, st>>>(w->b.keys[w->sort_final], w->b.vals[w->sort_final], n, n,
-                                             w->b.id[w->cur_id], w->b.h[w->cur_h], w->b.type_bitmap,
-                                             w->b.counts, w->b.word, ks.continentalCrustThreshold,
-                                             ks.collisionTypeUpdateCooldown);
+    const uint32_t n = (uint32_t)b.total;
+    const tecto_kernel_settings &ks = b.settings.kernel;
+    k_words<<<(n + 255) / 256, 256, 0, st>>>(b.keys[b.sort_final], b.vals[b.sort_final], n, b.d_worlds,
+                                             b.d_vbase, (int)b.members.size(), b.cur_id, b.cur_h,
+                                             ks.continentalCrustThreshold, ks.collisionTypeUpdateCooldown);
     TECTO_CUDA(cudaGetLastError());
-    w->launches += 1;
+    b.launches += 1;
     return TECTO_OK;
 }
 
-int launch_type_matrix(tecto_world *w, cudaStream_t st)
+int launch_type_matrix(Batch &b, cudaStream_t st)
 {
-    const tecto_kernel_settings &ks = w->settings.kernel;
-    k_type_matrix<<<(kPairs + 255) / 256, 256, 0, st>>>(w->b.counts, w->b.type_bitmap,
-                                                        ks.collisionTypeUpdateCooldown,
-                                                        ks.minCollisionSize);
+    const tecto_kernel_settings &ks = b.settings.kernel;
+    const dim3 grid((kPairs + 255) / 256, (unsigned)b.members.size());
+    k_type_matrix<<<grid, 256, 0, st>>>(b.d_worlds, ks.collisionTypeUpdateCooldown, ks.minCollisionSize);
     TECTO_CUDA(cudaGetLastError());
-    w->launches += 1;
+    b.launches += 1;
     return TECTO_OK;
 }
 

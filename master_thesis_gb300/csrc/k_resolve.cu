@@ -13,23 +13,28 @@ constexpr int RY = 16;   // resolve tile height
 constexpr int kMaxBlurRadius = 8;
 
 struct ResolveParams {
-    int W, H;
-    const uint32_t *word;
-    const uint8_t *id_old;
-    const float *h_old;
-    const int2 *off;
-    const uint8_t *bm;
-    const uint32_t *div_bitmap;
-    uint32_t *has_div;
-    float *h_new;
-    uint8_t *id_new;
-    unsigned long long *acc;
-    uint32_t *acc_list;
-    Control *ctl;
+    const WorldDev *worlds;
+    const uint2 *tiles;
+    int cur_h, cur_id;
     float thr;
     float tmin, tmax, tfac;
     float amount;
     float wts[2 * kMaxBlurRadius + 1];
+};
+
+// One world's view inside the resolve kernel.
+struct ResolveWorld {
+    int W, H;
+    uint32_t vbase;
+    const uint32_t *word;
+    const uint8_t *id_old;
+    const float *h_old;
+    const uint8_t *bm;
+    const uint32_t *div_bitmap;
+    uint32_t *has_div;
+    unsigned long long *acc;
+    uint32_t *acc_list;
+    uint32_t *acc_count;
 };
 
 // determineCollisionType device function (:611-649)
@@ -49,42 +54,42 @@ __device__ __forceinline__ uint32_t pair_type(const uint8_t *bm, uint8_t A, uint
     return out;
 }
 
-__device__ __forceinline__ void mark_accretion(const ResolveParams &p, uint32_t target, uint32_t d,
-                                               uint8_t owner)
+__device__ __forceinline__ void mark_accretion(const ResolveParams &p, const ResolveWorld &w,
+                                               uint32_t target, uint32_t d, uint8_t owner)
 {
     // last writer in cell order wins (the reference writes the byte plainly, :531-555)
     const unsigned long long v = ((unsigned long long)(d + 1u) << 8) | (unsigned long long)(255u - owner);
-    const unsigned long long old = atomicMax(p.acc + target, v);
+    const unsigned long long old = atomicMax(w.acc + target, v);
     if (old == 0ull) {
-        const uint32_t slot = atomicAdd(&p.ctl->acc_count, 1u);
-        p.acc_list[slot] = target;
+        const uint32_t slot = atomicAdd(w.acc_count, 1u);
+        w.acc_list[slot] = target;
     }
 }
 
 // Resolve one destination cell d = (x, y); returns the new height (before uplift).
-__device__ __forceinline__ float resolve_cell(const ResolveParams &p, const int2 *s_off, int x, int y,
-                                              uint32_t d, uint32_t cv, uint32_t seed,
-                                              uint32_t iteration, uint8_t *id_out)
+__device__ __forceinline__ float resolve_cell(const ResolveParams &p, const ResolveWorld &w,
+                                              const int2 *s_off, int x, int y, uint32_t d, uint32_t cv,
+                                              uint32_t seed, uint32_t iteration, uint8_t *id_out)
 {
-    const int W = p.W, H = p.H;
+    const int W = w.W, H = w.H;
     if (cv == 0u) {
         // processDivergence (:301-362)
-        const uint8_t prev = p.id_old[d];
+        const uint8_t prev = w.id_old[d];
         const int2 o = s_off[prev];
-        const uint32_t cvo = p.word[cidx(x - o.x, y - o.y, W, H)];
+        const uint32_t cvo = w.word[cidx(x - o.x, y - o.y, W, H)];
         const uint8_t oppId = (uint8_t)((255u - cvo) & 0xFFu);
         uint8_t nid = prev;
         if (cvo != 0u && cvo <= 0xFFu && oppId != prev) {
             const uint8_t mn = prev < oppId ? prev : oppId;
             const uint8_t mx = prev < oppId ? oppId : prev;
             const uint32_t bit = tri_index(mn, mx);
-            nid = (__ldg(p.div_bitmap + bit / 32u) & (1u << (bit % 32u))) ? mn : mx;
-            atomicOr(p.has_div + bit / 32u, 1u << (bit % 32u));
+            nid = (__ldg(w.div_bitmap + bit / 32u) & (1u << (bit % 32u))) ? mn : mx;
+            atomicOr(w.has_div + bit / 32u, 1u << (bit % 32u));
         }
         const float noise = simplex3((float)x, (float)y, (float)iteration, 0.01f, (int)seed);
         const float target = p.tmin + noise * (p.tmax - p.tmin);
         *id_out = nid;
-        return lerp_p0811(p.h_old[d], target, p.tfac);
+        return lerp_p0811(w.h_old[d], target, p.tfac);
     }
     uint8_t ids[4];
 #pragma unroll
@@ -93,7 +98,7 @@ __device__ __forceinline__ float resolve_cell(const ResolveParams &p, const int2
         // processMovement (:586-609)
         const int2 o = s_off[ids[0]];
         *id_out = ids[0];
-        return p.h_old[cidx(x - o.x, y - o.y, W, H)];
+        return w.h_old[cidx(x - o.x, y - o.y, W, H)];
     }
     // processConvergence (:469-584)
     const int n = ids[3] != 255 ? 4 : ids[2] != 255 ? 3 : 2;
@@ -103,12 +108,12 @@ __device__ __forceinline__ float resolve_cell(const ResolveParams &p, const int2
     float heights[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     for (int k = 0; k < n; ++k) {
         const int2 o = s_off[ids[k]];
-        heights[k] = p.h_old[cidx(x - o.x, y - o.y, W, H)];
+        heights[k] = w.h_old[cidx(x - o.x, y - o.y, W, H)];
     }
     uint32_t types[6];
     bool sub[4] = {false, false, false, false};
     for (int a = 0; a < pairLen; ++a) {
-        types[a] = pair_type(p.bm, ids[PA[a]], ids[PB[a]], heights[PA[a]], heights[PB[a]], p.thr);
+        types[a] = pair_type(w.bm, ids[PA[a]], ids[PB[a]], heights[PA[a]], heights[PB[a]], p.thr);
         if (types[a] == 1u || types[a] == 3u) sub[PA[a]] = true;
         else if (types[a] == 2u || types[a] == 4u) sub[PB[a]] = true;
     }
@@ -136,7 +141,7 @@ __device__ __forceinline__ float resolve_cell(const ResolveParams &p, const int2
                 const int2 ow = s_off[ownerId];
                 target = cidx(x + ow.x, y + ow.y, W, H);
             }
-            mark_accretion(p, target, d, ownerId);
+            mark_accretion(p, w, target, d, ownerId);
         }
     }
     *id_out = ownerId;
@@ -150,13 +155,31 @@ __global__ __launch_bounds__(256) void k_resolve(ResolveParams p)
     __shared__ uint32_t s_word[SY * SX];
     __shared__ float s_tmp[(R > 0) ? SY * RX : 1];
     __shared__ int2 s_off[kPlates + 1];
+    int wi, tx, ty;
+    tile_of(p.tiles[blockIdx.x], &wi, &tx, &ty);
+    const WorldDev &wd = p.worlds[wi];
+    ResolveWorld w;
+    w.W = wd.W;
+    w.H = wd.H;
+    w.vbase = wd.vbase;
+    w.word = wd.word;
+    w.id_old = wd.id[p.cur_id];
+    w.h_old = wd.h[p.cur_h];
+    w.bm = wd.type_bitmap;
+    w.div_bitmap = wd.div_bitmap;
+    w.has_div = wd.has_div;
+    w.acc = wd.acc;
+    w.acc_list = wd.acc_list;
+    w.acc_count = &wd.ctl->acc_count;
+    float *h_new = wd.h[p.cur_h ^ 1];
+    uint8_t *id_new = wd.id[p.cur_id ^ 1];
     const int t = threadIdx.x;
-    const int x0 = blockIdx.x * RX, y0 = blockIdx.y * RY;
-    for (int i = t; i < kPlates + 1; i += 256) s_off[i] = p.off[i];
+    const int x0 = tx * RX, y0 = ty * RY;
+    for (int i = t; i < kPlates + 1; i += 256) s_off[i] = wd.off[i];
     for (int e = t; e < SY * SX; e += 256) {
         const int ly = e / SX, lx = e - ly * SX;
-        const int gx = wrap_fast(x0 + lx - R, p.W), gy = wrap_fast(y0 + ly - R, p.H);
-        s_word[e] = p.word[(size_t)gy * p.W + gx];
+        const int gx = wrap_fast(x0 + lx - R, w.W), gy = wrap_fast(y0 + ly - R, w.H);
+        s_word[e] = w.word[(size_t)gy * w.W + gx];
     }
     __syncthreads();
     if (R > 0) {
@@ -173,62 +196,68 @@ __global__ __launch_bounds__(256) void k_resolve(ResolveParams p)
         }
         __syncthreads();
     }
-    const uint32_t seed = p.ctl->seed, iteration = p.ctl->iteration;
+    const uint32_t seed = wd.ctl->seed, iteration = wd.ctl->iteration;
     const int lx = t % RX;
 #pragma unroll 1
     for (int ly = t / RX; ly < RY; ly += 256 / RX) {
         const int x = x0 + lx, y = y0 + ly;
-        if (x >= p.W || y >= p.H) continue;
-        const uint32_t d = (uint32_t)y * (uint32_t)p.W + (uint32_t)x;
+        if (x >= w.W || y >= w.H) continue;
+        const uint32_t d = (uint32_t)y * (uint32_t)w.W + (uint32_t)x;
         const uint32_t cv = s_word[(ly + R) * SX + lx + R];
         uint8_t nid;
-        float hn = resolve_cell(p, s_off, x, y, d, cv, seed, iteration, &nid);
+        float hn = resolve_cell(p, w, s_off, x, y, d, cv, seed, iteration, &nid);
         if (R > 0) {
             float a = 0.0f;
 #pragma unroll
             for (int k = -R; k <= R; ++k) a = a + p.wts[k + R] * s_tmp[(ly + R + k) * RX + lx];
             hn = hn + a;
         }
-        p.h_new[d] = hn;
-        p.id_new[d] = nid;
+        h_new[d] = hn;
+        id_new[d] = nid;
     }
 }
 
-// flipDivergedBitmap (:772-780); clears the per-step bits for the next step
-__global__ void k_flip(uint32_t *div_bitmap, uint32_t *has_div)
+// flipDivergedBitmap (:772-780) for every world; clears the per-step bits for the next step
+__global__ void k_flip(const WorldDev *worlds)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < kDivWords) {
-        div_bitmap[i] ^= has_div[i];
-        has_div[i] = 0u;
+        const WorldDev &wd = worlds[blockIdx.y];
+        wd.div_bitmap[i] ^= wd.has_div[i];
+        wd.has_div[i] = 0u;
     }
 }
 
-// applyAccretion (:747-770) over the cells that received a mark this step; clears the marks and
-// advances the step counter.
-__global__ void k_finish(unsigned long long *acc, const uint32_t *acc_list, uint8_t *acc_u8,
-                         const float *h, uint8_t *id, Control *ctl, float thr)
+// applyAccretion (:747-770) over the cells that received a mark this step; clears the marks.
+// Grid: (blocks, worlds).
+__global__ void k_finish(const WorldDev *worlds, int cur_h, int cur_id, float thr)
 {
-    const uint32_t count = ctl->acc_count;
+    const WorldDev &wd = worlds[blockIdx.y];
+    const uint32_t count = wd.ctl->acc_count;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-        const uint32_t c = acc_list[i];
-        const unsigned long long m = acc[c];
-        acc[c] = 0ull;
+        const uint32_t c = wd.acc_list[i];
+        const unsigned long long m = wd.acc[c];
+        wd.acc[c] = 0ull;
         const uint8_t value = (uint8_t)(m & 0xFFu);
-        acc_u8[c] = value;
+        wd.acc_u8[c] = value;
         const uint8_t accId = (uint8_t)(255u - value);
-        if (accId != 255 && h[c] >= thr) id[c] = accId;
+        if (accId != 255 && wd.h[cur_h][c] >= thr) wd.id[cur_id][c] = accId;
     }
 }
 
-__global__ void k_bump_iteration(Control *ctl) { ctl->iteration += 1u; }
-
-// Clears last step's decoded marks before this step's resolve (list of the previous step).
-__global__ void k_clear_acc_u8(uint8_t *acc_u8, const uint32_t *acc_list, const Control *ctl)
+__global__ void k_bump_iteration(const WorldDev *worlds, int nworlds)
 {
-    const uint32_t count = ctl->acc_count;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nworlds) worlds[i].ctl->iteration += 1u;
+}
+
+// Clears the previous step's decoded marks before this step's resolve.  Grid: (blocks, worlds).
+__global__ void k_clear_acc_u8(const WorldDev *worlds)
+{
+    const WorldDev &wd = worlds[blockIdx.y];
+    const uint32_t count = wd.ctl->acc_count;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)
-        acc_u8[acc_list[i]] = 0;
+        wd.acc_u8[wd.acc_list[i]] = 0;
 }
 
 }  // namespace
@@ -244,24 +273,14 @@ void gaussian_weights(float sigma, int radius, float *out)
     for (int k = 0; k <= 2 * radius; ++k) out[k] = (float)(tmp[k] / sum);
 }
 
-int launch_resolve(tecto_world *w, cudaStream_t st)
+int launch_resolve(Batch &b, cudaStream_t st)
 {
-    const tecto_settings &s = w->settings;
+    const tecto_settings &s = b.settings;
     ResolveParams p{};
-    p.W = w->W;
-    p.H = w->H;
-    p.word = w->b.word;
-    p.id_old = w->b.id[w->cur_id];
-    p.h_old = w->b.h[w->cur_h];
-    p.off = w->b.off;
-    p.bm = w->b.type_bitmap;
-    p.div_bitmap = w->b.div_bitmap;
-    p.has_div = w->b.has_div;
-    p.h_new = w->b.h[w->cur_h ^ 1];
-    p.id_new = w->b.id[w->cur_id ^ 1];
-    p.acc = w->b.acc;
-    p.acc_list = w->b.acc_list;
-    p.ctl = w->b.ctl;
+    p.worlds = b.d_worlds;
+    p.tiles = b.d_tiles[TK_RESOLVE];
+    p.cur_h = b.cur_h;
+    p.cur_id = b.cur_id;
     p.thr = s.kernel.continentalCrustThreshold;
     p.tmin = s.kernel.divergence_height_target_min;
     p.tmax = s.kernel.divergence_height_target_max;
@@ -276,7 +295,7 @@ int launch_resolve(tecto_world *w, cudaStream_t st)
         }
         gaussian_weights(s.step.upliftSigma, R, p.wts);
     }
-    const dim3 grid((unsigned)((w->W + RX - 1) / RX), (unsigned)((w->H + RY - 1) / RY));
+    const unsigned grid = (unsigned)b.ntiles[TK_RESOLVE];
     switch (R) {
         case 0: k_resolve<0><<<grid, 256, 0, st>>>(p); break;
         case 1: k_resolve<1><<<grid, 256, 0, st>>>(p); break;
@@ -288,38 +307,38 @@ int launch_resolve(tecto_world *w, cudaStream_t st)
         case 7: k_resolve<7><<<grid, 256, 0, st>>>(p); break;
         default: k_resolve<8><<<grid, 256, 0, st>>>(p); break;
     }
-    k_flip<<<(kDivWords + 255) / 256, 256, 0, st>>>(w->b.div_bitmap, w->b.has_div);
+    k_flip<<<dim3((kDivWords + 255) / 256, (unsigned)b.members.size()), 256, 0, st>>>(b.d_worlds);
     TECTO_CUDA(cudaGetLastError());
-    w->launches += 2;
-    w->cur_h ^= 1;
-    w->cur_id ^= 1;
+    b.launches += 2;
+    b.cur_h ^= 1;
+    b.cur_id ^= 1;
     return TECTO_OK;
 }
 
-int launch_finish(tecto_world *w, cudaStream_t st)
+int launch_finish(Batch &b, cudaStream_t st)
 {
-    k_finish<<<152, 256, 0, st>>>(w->b.acc, w->b.acc_list, w->b.acc_u8, w->b.h[w->cur_h],
-                                  w->b.id[w->cur_id], w->b.ctl,
-                                  w->settings.kernel.continentalCrustThreshold);
+    k_finish<<<dim3(4, (unsigned)b.members.size()), 256, 0, st>>>(b.d_worlds, b.cur_h, b.cur_id,
+                                                                   b.settings.kernel.continentalCrustThreshold);
     TECTO_CUDA(cudaGetLastError());
-    w->launches += 1;
+    b.launches += 1;
     return TECTO_OK;
 }
 
 // Runs before launch_plates resets the list count: clears the previous step's decoded marks.
-int launch_clear_marks(tecto_world *w, cudaStream_t st)
+int launch_clear_marks(Batch &b, cudaStream_t st)
 {
-    k_clear_acc_u8<<<64, 256, 0, st>>>(w->b.acc_u8, w->b.acc_list, w->b.ctl);
+    k_clear_acc_u8<<<dim3(4, (unsigned)b.members.size()), 256, 0, st>>>(b.d_worlds);
     TECTO_CUDA(cudaGetLastError());
-    w->launches += 1;
+    b.launches += 1;
     return TECTO_OK;
 }
 
-int launch_bump_iteration(tecto_world *w, cudaStream_t st)
+int launch_bump_iteration(Batch &b, cudaStream_t st)
 {
-    k_bump_iteration<<<1, 1, 0, st>>>(w->b.ctl);
+    const int n = (int)b.members.size();
+    k_bump_iteration<<<(n + 255) / 256, 256, 0, st>>>(b.d_worlds, n);
     TECTO_CUDA(cudaGetLastError());
-    w->launches += 1;
+    b.launches += 1;
     return TECTO_OK;
 }
 

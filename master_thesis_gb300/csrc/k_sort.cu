@@ -20,14 +20,30 @@ namespace {
 constexpr int kRadix = 256;
 constexpr int kWarps = kSortThreads / 32;
 
-__device__ __forceinline__ uint32_t gen_key(size_t i, const uint8_t *id, const int2 *s_off, int W,
-                                            int H)
+// Batch-virtual destination of virtual cell i: the owning world's getPixelMovements destination
+// (plate_tectonics_kernel.cu:248-265) offset by the world's virtual base.
+struct GenArgs {
+    const WorldDev *worlds;
+    const uint32_t *vbase;
+    int nworlds;
+    int cur_id;
+};
+
+__device__ __forceinline__ uint32_t gen_key(size_t i, const GenArgs &g, const uint32_t *s_vbase)
 {
-    const uint32_t i32 = (uint32_t)i;  // n < 2^30: 32-bit division is enough
-    const int y = (int)(i32 / (uint32_t)W);
-    const int x = (int)(i32 - (uint32_t)y * (uint32_t)W);
-    const int2 o = s_off[id[i]];
-    return cidx(x + o.x, y + o.y, W, H);
+    const uint32_t v = (uint32_t)i;  // n < 2^30
+    const WorldDev &wd = g.worlds[find_world(s_vbase, g.nworlds, v)];
+    const uint32_t local = v - wd.vbase;
+    const int W = wd.W;
+    const int y = (int)(local / (uint32_t)W);
+    const int x = (int)(local - (uint32_t)y * (uint32_t)W);
+    const int2 o = wd.off[wd.id[g.cur_id][local]];
+    return wd.vbase + cidx(x + o.x, y + o.y, W, wd.H);
+}
+
+__device__ __forceinline__ void load_vbase(const GenArgs &g, uint32_t *s_vbase)
+{
+    for (int i = threadIdx.x; i < g.nworlds; i += blockDim.x) s_vbase[i] = g.vbase[i];
 }
 
 __device__ __forceinline__ uint32_t ld_volatile(const uint32_t *p)
@@ -42,15 +58,13 @@ __device__ __forceinline__ void st_volatile(uint32_t *p, uint32_t v)
 
 // Digit histograms of all passes in one read of the keys.
 template <bool GEN>
-__global__ __launch_bounds__(256) void k_sort_hist(const uint8_t *gen_id, const int2 *gen_off,
-                                                   int W, int H, const uint32_t *keys_in, size_t n,
+__global__ __launch_bounds__(256) void k_sort_hist(GenArgs g, const uint32_t *keys_in, size_t n,
                                                    int passes, uint32_t *hist)
 {
     __shared__ uint32_t s_hist[kMaxSortPasses][kRadix];
-    __shared__ int2 s_off[kPlates + 1];
+    __shared__ uint32_t s_vbase[GEN ? kMaxBatchWorlds : 1];
     for (int i = threadIdx.x; i < kMaxSortPasses * kRadix; i += blockDim.x) (&s_hist[0][0])[i] = 0;
-    if (GEN)
-        for (int i = threadIdx.x; i < kPlates + 1; i += blockDim.x) s_off[i] = gen_off[i];
+    if (GEN) load_vbase(g, s_vbase);
     __syncthreads();
     const unsigned lane = threadIdx.x & 31u;
     const size_t stride = (size_t)gridDim.x * blockDim.x;
@@ -60,7 +74,7 @@ __global__ __launch_bounds__(256) void k_sort_hist(const uint8_t *gen_id, const 
         const size_t i = r * stride + (size_t)blockIdx.x * blockDim.x + threadIdx.x;
         const bool valid = i < n;
         uint32_t key = 0;
-        if (valid) key = GEN ? gen_key(i, gen_id, s_off, W, H) : keys_in[i];
+        if (valid) key = GEN ? gen_key(i, g, s_vbase) : keys_in[i];
         for (int p = 0; p < passes; ++p) {
             const uint32_t d = valid ? ((key >> (8 * p)) & 0xFFu) : 0x100u;
             const unsigned peers = __match_any_sync(0xffffffffu, d);
@@ -99,7 +113,7 @@ __global__ void k_sort_scan(uint32_t *hist, int passes)
 // One onesweep pass.
 template <bool GEN>
 __global__ __launch_bounds__(kSortThreads) void k_sort_pass(
-    const uint8_t *gen_id, const int2 *gen_off, int W, int H, const uint32_t *keys_in,
+    GenArgs g, const uint32_t *keys_in,
     const uint32_t *vals_in, uint32_t *keys_out, uint32_t *vals_out, size_t n, int shift,
     const uint32_t *digit_start, uint32_t *status, uint32_t *tile_counter, uint32_t *error)
 {
@@ -108,15 +122,14 @@ __global__ __launch_bounds__(kSortThreads) void k_sort_pass(
     __shared__ uint32_t s_base[kRadix];         // global output position of the digit's run
     __shared__ uint32_t s_keys[kSortTile];
     __shared__ uint32_t s_vals[kSortTile];
-    __shared__ int2 s_off[kPlates + 1];
+    __shared__ uint32_t s_vbase[GEN ? kMaxBatchWorlds : 1];
     __shared__ uint32_t s_wsum[kWarps];
     __shared__ uint32_t s_tile;
 
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     if (t == 0) s_tile = atomicAdd(tile_counter, 1u);
     for (int i = t; i < kWarps * kRadix; i += kSortThreads) (&s_cnt[0][0])[i] = 0;
-    if (GEN)
-        for (int i = t; i < kPlates + 1; i += kSortThreads) s_off[i] = gen_off[i];
+    if (GEN) load_vbase(g, s_vbase);
     __syncthreads();
     const uint32_t tile = s_tile;
     const size_t base = (size_t)tile * kSortTile;
@@ -128,7 +141,7 @@ __global__ __launch_bounds__(kSortThreads) void k_sort_pass(
         const size_t idx = wbase + (size_t)it * 32 + lane;
         if (idx < n) {
             if (GEN) {
-                k[it] = gen_key(idx, gen_id, s_off, W, H);
+                k[it] = gen_key(idx, g, s_vbase);
                 v[it] = (uint32_t)idx;
             } else {
                 k[it] = keys_in[idx];
@@ -281,14 +294,19 @@ int run_sort(const SortArgs &a, const SortScratch &scr, cudaStream_t st, int *re
     const size_t clear = align256((size_t)passes * kRadix * 4) +
                          align256((size_t)passes * tiles * kRadix * 4) + align256(kMaxSortPasses * 4);
     TECTO_CUDA(cudaMemsetAsync(scr.hist, 0, clear, st));
-    const bool gen = a.gen_id != nullptr;
+    const bool gen = a.worlds != nullptr;
+    const GenArgs g{a.worlds, a.vbase, a.nworlds, a.cur_id};
+    if (gen && (a.nworlds < 1 || a.nworlds > kMaxBatchWorlds)) {
+        set_error("run_sort: batch world count out of range");
+        return TECTO_ERR_INVALID;
+    }
     int hist_blocks = (int)((a.n + 255) / 256);
     if (hist_blocks > 152 * 8) hist_blocks = 152 * 8;
     if (gen)
-        k_sort_hist<true><<<hist_blocks, 256, 0, st>>>(a.gen_id, a.gen_off, a.W, a.H, nullptr, a.n,
+        k_sort_hist<true><<<hist_blocks, 256, 0, st>>>(g, nullptr, a.n,
                                                         passes, scr.hist);
     else
-        k_sort_hist<false><<<hist_blocks, 256, 0, st>>>(nullptr, nullptr, a.W, a.H, a.keys_in, a.n,
+        k_sort_hist<false><<<hist_blocks, 256, 0, st>>>(g, a.keys_in, a.n,
                                                          passes, scr.hist);
     k_sort_scan<<<1, kRadix, 0, st>>>(scr.hist, passes);
     int half = 0;
@@ -298,11 +316,11 @@ int run_sort(const SortArgs &a, const SortScratch &scr, cudaStream_t st, int *re
         uint32_t *status = scr.status + (size_t)p * tiles * kRadix;
         if (p == 0 && gen)
             k_sort_pass<true><<<(unsigned)tiles, kSortThreads, 0, st>>>(
-                a.gen_id, a.gen_off, a.W, a.H, nullptr, nullptr, kout, vout, a.n, 0, scr.hist,
+                g, nullptr, nullptr, kout, vout, a.n, 0, scr.hist,
                 status, scr.counters + p, scr.error);
         else
             k_sort_pass<false><<<(unsigned)tiles, kSortThreads, 0, st>>>(
-                nullptr, nullptr, a.W, a.H, kin, vin, kout, vout, a.n, 8 * p,
+                g, kin, vin, kout, vout, a.n, 8 * p,
                 scr.hist + p * kRadix, status, scr.counters + p, scr.error);
         kin = kout;
         vin = vout;

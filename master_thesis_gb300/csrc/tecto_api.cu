@@ -1,7 +1,7 @@
-// tecto_api.cu - the C ABI: world lifecycle and HBM arena, synthetic world generator, field I/O,
-// phase entry points and the step driver with CUDA-graph replay.
-// Replaces PlateTectonicSim (src/cuda_compute/plate_tectonic_sim.h:110-130,
-// plate_tectonic_sim.cu:28-131) for the hot-path phases.
+// tecto_api.cu - the C ABI for single worlds: lifecycle and HBM arena, synthetic world
+// generator, field I/O, phase entry points and the step driver.  Replaces PlateTectonicSim
+// (src/cuda_compute/plate_tectonic_sim.h:110-130, plate_tectonic_sim.cu:28-131) for the
+// hot-path phases.  A world stepped on its own runs as a private batch of one (tecto_batch.cu).
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -29,13 +29,10 @@ inline float u01(uint64_t r) { return (float)(r >> 40) * (1.0f / 16777216.0f); }
 
 // Device-side world layout: every buffer of the world in one allocation.
 struct Layout {
-    size_t off[40];
-    int n = 0;
     size_t total = 0;
     size_t add(size_t bytes)
     {
         const size_t o = total;
-        off[n++] = o;
         total += align256(bytes);
         return o;
     }
@@ -50,28 +47,6 @@ int check_world(const tecto_world *w)
     return TECTO_OK;
 }
 
-void field_info(tecto_world *w, int field, void **ptr, size_t *bytes)
-{
-    const size_t N = w->N;
-    *ptr = nullptr;
-    *bytes = 0;
-    switch (field) {
-        case TECTO_FIELD_HEIGHT: *ptr = w->b.h[w->cur_h]; *bytes = N * 4; break;
-        case TECTO_FIELD_WATER: *ptr = w->b.w[w->cur_wsf]; *bytes = N * 4; break;
-        case TECTO_FIELD_SEDIMENT: *ptr = w->b.s[w->cur_wsf]; *bytes = N * 4; break;
-        case TECTO_FIELD_FLUX: *ptr = w->b.flux[w->cur_wsf]; *bytes = N * 16; break;
-        case TECTO_FIELD_PLATE_ID: *ptr = w->b.id[w->cur_id]; *bytes = N; break;
-        case TECTO_FIELD_LABELS: *ptr = w->b.labels; *bytes = N * 4; break;
-        case TECTO_FIELD_COLLISION: *ptr = w->b.word; *bytes = N * 4; break;
-        case TECTO_FIELD_TYPE_BITMAP: *ptr = w->b.type_bitmap; *bytes = kPairs; break;
-        case TECTO_FIELD_DIV_BITMAP: *ptr = w->b.div_bitmap; *bytes = kDivWords * 4; break;
-        case TECTO_FIELD_SORT_KEYS: *ptr = w->b.keys[w->sort_final]; *bytes = N * 4; break;
-        case TECTO_FIELD_SORT_VALS: *ptr = w->b.vals[w->sort_final]; *bytes = N * 4; break;
-        case TECTO_FIELD_ACCRETION: *ptr = w->b.acc_u8; *bytes = N; break;
-        default: break;
-    }
-}
-
 int bind_device(const tecto_world *w)
 {
     int cur = -1;
@@ -80,49 +55,65 @@ int bind_device(const tecto_world *w)
     return TECTO_OK;
 }
 
-void drop_graphs(tecto_world *w)
+// The world's private batch of one, aligned with the world's current ping-pong halves.  Fails
+// while the world belongs to a public batch (its state is then stepped by that batch).
+int own_batch(tecto_world *w, Batch **out)
 {
-    for (int i = 0; i < 16; ++i) {
-        if (w->graph_valid[i]) cudaGraphExecDestroy(w->graphs[i]);
-        w->graph_valid[i] = false;
+    if (w->in_batch && w->in_batch != w->own) {
+        set_error("world belongs to a batch: step it through tecto_batch_step or remove it first");
+        return TECTO_ERR_INVALID;
     }
+    if (!w->own) {
+        w->own = new (std::nothrow) Batch();
+        if (!w->own) return TECTO_ERR_OOM;
+        const int rc = batch_join(*w->own, w, nullptr);
+        if (rc != TECTO_OK) return rc;
+    }
+    Batch &b = *w->own;
+    if (std::memcmp(&b.settings, &w->settings, sizeof(tecto_settings)) != 0) {
+        b.settings = w->settings;
+        b.dirty = true;
+    }
+    b.cur_h = w->cur_h;
+    b.cur_wsf = w->cur_wsf;
+    b.cur_id = w->cur_id;
+    w->in_batch = w->own;
+    *out = w->own;
+    return batch_prepare(b, nullptr);
 }
 
-int enqueue_collide(tecto_world *w, cudaStream_t st)
+void from_batch(tecto_world *w, const Batch &b)
 {
-    int rc;
-    if ((rc = launch_plates(w, st)) != TECTO_OK) return rc;
-    if ((rc = launch_sort_keys(w, st)) != TECTO_OK) return rc;
-    if ((rc = launch_words(w, st)) != TECTO_OK) return rc;
-    return launch_type_matrix(w, st);
+    w->cur_h = b.cur_h;
+    w->cur_wsf = b.cur_wsf;
+    w->cur_id = b.cur_id;
 }
 
-bool ccl_due(const tecto_world *w)
+void field_info(tecto_world *w, int field, void **ptr, size_t *bytes)
 {
-    const int period = w->settings.sim.iterationsForCCL > 0 ? w->settings.sim.iterationsForCCL : 1;
-    return w->iteration % (uint32_t)period == 0;
-}
-
-int enqueue_finish(tecto_world *w, cudaStream_t st, bool ccl)
-{
-    int rc;
-    if ((rc = launch_finish(w, st)) != TECTO_OK) return rc;
-    if (ccl && (rc = launch_ccl(w, w->settings.step.cclConnectivity, st)) != TECTO_OK) return rc;
-    if ((rc = launch_bump_iteration(w, st)) != TECTO_OK) return rc;
-    w->iteration += 1;
-    return TECTO_OK;
-}
-
-int enqueue_step(tecto_world *w, cudaStream_t st, bool ccl)
-{
-    int rc;
-    if ((rc = enqueue_collide(w, st)) != TECTO_OK) return rc;
-    if ((rc = launch_resolve(w, st)) != TECTO_OK) return rc;
-    if ((rc = launch_thermal(w, w->settings.step.thermalIterations, st)) != TECTO_OK) return rc;
-    if ((rc = launch_hydraulic(w, w->settings.step.hydraulicIterations, w->settings.step.hydraulicDt,
-                               st)) != TECTO_OK)
-        return rc;
-    return enqueue_finish(w, st, ccl);
+    const size_t N = w->N;
+    const WorldDev &d = w->dev;
+    *ptr = nullptr;
+    *bytes = 0;
+    switch (field) {
+        case TECTO_FIELD_HEIGHT: *ptr = d.h[w->cur_h]; *bytes = N * 4; break;
+        case TECTO_FIELD_WATER: *ptr = d.w[w->cur_wsf]; *bytes = N * 4; break;
+        case TECTO_FIELD_SEDIMENT: *ptr = d.s[w->cur_wsf]; *bytes = N * 4; break;
+        case TECTO_FIELD_FLUX: *ptr = d.flux[w->cur_wsf]; *bytes = N * 16; break;
+        case TECTO_FIELD_PLATE_ID: *ptr = d.id[w->cur_id]; *bytes = N; break;
+        case TECTO_FIELD_LABELS: *ptr = d.labels; *bytes = N * 4; break;
+        case TECTO_FIELD_COLLISION: *ptr = d.word; *bytes = N * 4; break;
+        case TECTO_FIELD_TYPE_BITMAP: *ptr = d.type_bitmap; *bytes = kPairs; break;
+        case TECTO_FIELD_DIV_BITMAP: *ptr = d.div_bitmap; *bytes = kDivWords * 4; break;
+        case TECTO_FIELD_SORT_KEYS:
+            if (w->own && w->own->arena) { *ptr = w->own->keys[w->own->sort_final]; *bytes = N * 4; }
+            break;
+        case TECTO_FIELD_SORT_VALS:
+            if (w->own && w->own->arena) { *ptr = w->own->vals[w->own->sort_final]; *bytes = N * 4; }
+            break;
+        case TECTO_FIELD_ACCRETION: *ptr = d.acc_u8; *bytes = N; break;
+        default: break;
+    }
 }
 
 }  // namespace
@@ -135,7 +126,19 @@ int cuda_fail(cudaError_t e, const char *what)
     return e == cudaErrorMemoryAllocation ? TECTO_ERR_OOM : TECTO_ERR_CUDA;
 }
 
-int ensure_kernel_attributes();
+// Bytes of device memory one world of W x H cells holds (its arena, and its share of the
+// batch-level buffers: sort keys/values, accretion list, sort status).
+size_t world_footprint(int W, int H)
+{
+    const size_t N = (size_t)W * (size_t)H;
+    Layout L;
+    L.add(N * 4); L.add(N * 4); L.add(N * 4); L.add(N * 4); L.add(N * 4); L.add(N * 4);
+    L.add(N * 16); L.add(N * 16); L.add(N); L.add(N);
+    L.add(N * 4); L.add(N * 4); L.add(N * 4); L.add(N * 8); L.add(N * 4); L.add(N * 8); L.add(N * 4); L.add(N);
+    L.add(kPairs); L.add(kDivWords * 4); L.add(kDivWords * 4); L.add(kPairs * sizeof(PairCounts));
+    L.add(kPlates * sizeof(tecto_plate)); L.add((kPlates + 1) * sizeof(int2)); L.add(sizeof(Control));
+    return L.total + 4 * N * 4 + sort_scratch_bytes(N, 32) / 2;
+}
 
 }  // namespace tecto
 
@@ -145,7 +148,13 @@ extern "C" {
 
 const char *tecto_last_error_string(void) { return g_last_error.c_str(); }
 
-const char *tecto_version(void) { return "tecto-gb300 0.1 (sm_103a)"; }
+const char *tecto_version(void) { return "tecto-gb300 0.2 (sm_103a)"; }
+
+size_t tecto_world_bytes(int width, int height)
+{
+    if (width < 1 || height < 1) return 0;
+    return world_footprint(width, height);
+}
 
 int tecto_world_create(const tecto_settings *settings, int width, int height, uint32_t seed,
                        tecto_world **out)
@@ -168,7 +177,6 @@ int tecto_world_create(const tecto_settings *settings, int width, int height, ui
     w->settings = *settings;
     w->seed = seed;
     cudaGetDevice(&w->device);
-    const int kb = key_bits_for(N);
     Layout L;
     const size_t o_h0 = L.add(N * 4), o_h1 = L.add(N * 4);
     const size_t o_w0 = L.add(N * 4), o_w1 = L.add(N * 4);
@@ -176,8 +184,6 @@ int tecto_world_create(const tecto_settings *settings, int width, int height, ui
     const size_t o_f0 = L.add(N * 16), o_f1 = L.add(N * 16);
     const size_t o_i0 = L.add(N), o_i1 = L.add(N);
     const size_t o_word = L.add(N * 4);
-    const size_t o_k0 = L.add(N * 4), o_k1 = L.add(N * 4);
-    const size_t o_v0 = L.add(N * 4), o_v1 = L.add(N * 4);
     const size_t o_lab = L.add(N * 4);
     const size_t o_rain = L.add(N * 4);
     const size_t o_vel = L.add(N * 8);
@@ -192,7 +198,6 @@ int tecto_world_create(const tecto_settings *settings, int width, int height, ui
     const size_t o_pl = L.add(kPlates * sizeof(tecto_plate));
     const size_t o_off = L.add((kPlates + 1) * sizeof(int2));
     const size_t o_ctl = L.add(sizeof(Control));
-    const size_t o_sort = L.add(sort_scratch_bytes(N, kb));
     cudaError_t e = cudaMalloc(&w->arena, L.total);
     if (e != cudaSuccess) {
         delete w;
@@ -200,42 +205,41 @@ int tecto_world_create(const tecto_settings *settings, int width, int height, ui
     }
     w->arena_bytes = L.total;
     char *base = (char *)w->arena;
-    WorldBuffers &b = w->b;
-    b.h[0] = (float *)(base + o_h0);
-    b.h[1] = (float *)(base + o_h1);
-    b.w[0] = (float *)(base + o_w0);
-    b.w[1] = (float *)(base + o_w1);
-    b.s[0] = (float *)(base + o_s0);
-    b.s[1] = (float *)(base + o_s1);
-    b.flux[0] = (float4 *)(base + o_f0);
-    b.flux[1] = (float4 *)(base + o_f1);
-    b.id[0] = (uint8_t *)(base + o_i0);
-    b.id[1] = (uint8_t *)(base + o_i1);
-    b.word = (uint32_t *)(base + o_word);
-    b.keys[0] = (uint32_t *)(base + o_k0);
-    b.keys[1] = (uint32_t *)(base + o_k1);
-    b.vals[0] = (uint32_t *)(base + o_v0);
-    b.vals[1] = (uint32_t *)(base + o_v1);
-    b.labels = (uint32_t *)(base + o_lab);
-    b.rain = (float *)(base + o_rain);
-    b.vel = (float2 *)(base + o_vel);
-    b.s1 = (float *)(base + o_s1b);
-    b.acc = (unsigned long long *)(base + o_acc);
-    b.acc_list = (uint32_t *)(base + o_accl);
-    b.acc_u8 = (uint8_t *)(base + o_accu);
-    b.type_bitmap = (uint8_t *)(base + o_bm);
-    b.div_bitmap = (uint32_t *)(base + o_div);
-    b.has_div = (uint32_t *)(base + o_hd);
-    b.counts = (PairCounts *)(base + o_cnt);
-    b.plates = (tecto_plate *)(base + o_pl);
-    b.off = (int2 *)(base + o_off);
-    b.ctl = (Control *)(base + o_ctl);
-    sort_scratch_carve(base + o_sort, N, kb, &b.sort);
+    WorldDev &d = w->dev;
+    d.W = width;
+    d.H = height;
+    d.N = (uint32_t)N;
+    d.vbase = 0;
+    d.h[0] = (float *)(base + o_h0);
+    d.h[1] = (float *)(base + o_h1);
+    d.w[0] = (float *)(base + o_w0);
+    d.w[1] = (float *)(base + o_w1);
+    d.s[0] = (float *)(base + o_s0);
+    d.s[1] = (float *)(base + o_s1);
+    d.flux[0] = (float4 *)(base + o_f0);
+    d.flux[1] = (float4 *)(base + o_f1);
+    d.id[0] = (uint8_t *)(base + o_i0);
+    d.id[1] = (uint8_t *)(base + o_i1);
+    d.word = (uint32_t *)(base + o_word);
+    d.labels = (uint32_t *)(base + o_lab);
+    d.rain = (float *)(base + o_rain);
+    d.vel = (float2 *)(base + o_vel);
+    d.s1 = (float *)(base + o_s1b);
+    d.acc = (unsigned long long *)(base + o_acc);
+    d.acc_list = (uint32_t *)(base + o_accl);
+    d.acc_u8 = (uint8_t *)(base + o_accu);
+    d.type_bitmap = (uint8_t *)(base + o_bm);
+    d.div_bitmap = (uint32_t *)(base + o_div);
+    d.has_div = (uint32_t *)(base + o_hd);
+    d.counts = (PairCounts *)(base + o_cnt);
+    d.plates = (tecto_plate *)(base + o_pl);
+    d.off = (int2 *)(base + o_off);
+    d.ctl = (Control *)(base + o_ctl);
     e = cudaMemset(w->arena, 0, L.total);
     if (e == cudaSuccess) {
         Control c{};
         c.seed = seed;
-        e = cudaMemcpy(b.ctl, &c, sizeof(c), cudaMemcpyHostToDevice);
+        e = cudaMemcpy(d.ctl, &c, sizeof(c), cudaMemcpyHostToDevice);
     }
     if (e != cudaSuccess) {
         cudaFree(w->arena);
@@ -255,7 +259,12 @@ int tecto_world_create(const tecto_settings *settings, int width, int height, ui
 int tecto_world_destroy(tecto_world *w)
 {
     if (!w) return TECTO_OK;
-    drop_graphs(w);
+    if (w->in_batch && w->in_batch != w->own) batch_leave(*w->in_batch, w);
+    if (w->own) {
+        batch_release(*w->own);
+        delete w->own;
+        w->own = nullptr;
+    }
     if (w->arena) cudaFree(w->arena);
     w->arena = nullptr;
     delete w;
@@ -267,8 +276,11 @@ int tecto_world_set_settings(tecto_world *w, const tecto_settings *s)
     int rc = check_world(w);
     if (rc != TECTO_OK) return rc;
     if (!s) return TECTO_ERR_INVALID;
+    if (w->in_batch && w->in_batch != w->own) {
+        set_error("world belongs to a batch: remove it before changing its settings");
+        return TECTO_ERR_INVALID;
+    }
     w->settings = *s;
-    drop_graphs(w);
     return TECTO_OK;
 }
 
@@ -290,17 +302,19 @@ int tecto_world_size(const tecto_world *w, int *width, int *height)
     return TECTO_OK;
 }
 
-int tecto_generate_world_host(int W, int H, int P, float velRange, uint64_t genSeed, float *height_out,
-                              uint8_t *id_out, tecto_plate *plates_out)
+}  // extern "C"
+
+namespace tecto {
+namespace gen {
+
+// Seed points and plate kinematics of the synthetic generator (host, cheap: P <= 255).
+void gen_seeds(int W, int H, int P, float velRange, uint64_t genSeed, std::vector<float> &sx,
+               std::vector<float> &sy, std::vector<tecto_plate> &pl)
 {
-    if (W < 1 || H < 1 || P < 1 || P > kPlates) {
-        set_error("tecto_generate_world_host: invalid size or plate count (1..255)");
-        return TECTO_ERR_INVALID;
-    }
     uint64_t st = genSeed;
-    std::vector<float> sx(P), sy(P);
-    std::vector<tecto_plate> pl(kPlates);
-    std::memset(pl.data(), 0, sizeof(tecto_plate) * kPlates);
+    sx.assign(P, 0.0f);
+    sy.assign(P, 0.0f);
+    pl.assign(kPlates, tecto_plate{});
     for (int k = 0; k < P; ++k) {
         sx[k] = u01(splitmix64(st)) * (float)W;
         sy[k] = u01(splitmix64(st)) * (float)H;
@@ -313,6 +327,103 @@ int tecto_generate_world_host(int W, int H, int P, float velRange, uint64_t genS
         pl[k].pixelCenter_x = sx[k] - floorf(sx[k]);
         pl[k].pixelCenter_y = sy[k] - floorf(sy[k]);
     }
+}
+
+__device__ __forceinline__ uint64_t splitmix64_d(uint64_t &s)
+{
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// Per-cell part of the generator on the GPU, operation for operation the host loop below.
+__global__ void k_generate(float *h, uint8_t *id, int W, int H, int P, const float *sx, const float *sy,
+                           uint64_t genSeed)
+{
+    __shared__ float s_x[kPlates], s_y[kPlates];
+    for (int k = threadIdx.x; k < P; k += blockDim.x) {
+        s_x[k] = sx[k];
+        s_y[k] = sy[k];
+    }
+    __syncthreads();
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)W * (size_t)H) return;
+    const int y = (int)(i / (size_t)W), x = (int)(i - (size_t)y * W);
+    const float fW = (float)W, fH = (float)H;
+    float best = 3.4e38f;
+    int bid = 0;
+    for (int k = 0; k < P; ++k) {
+        const float dx = fabsf((float)x - s_x[k]), dy = fabsf((float)y - s_y[k]);
+        const float wx = fminf(dx, fW - dx), wy = fminf(dy, fH - dy);
+        const float d2 = wx * wx + wy * wy;
+        if (d2 < best) {
+            best = d2;
+            bid = k;
+        }
+    }
+    id[i] = (uint8_t)bid;
+    uint64_t cs = genSeed ^ (0xD1B54A32D192ED03ull * (uint64_t)(i + 1));
+    float sum = 0.0f;
+    for (int r = 0; r < 12; ++r) sum = sum + (float)(splitmix64_d(cs) >> 40) * (1.0f / 16777216.0f);
+    const float n = sum - 6.0f;
+    h[i] = (bid % 2 == 0) ? 0.5f + 0.05f * n : -0.5f + 0.02f * n;
+}
+
+}  // namespace gen
+}  // namespace tecto
+
+using namespace tecto::gen;
+
+extern "C" {
+
+int tecto_world_init_synthetic_device(tecto_world *w, int P, float velRange, uint64_t genSeed,
+                                      tecto_stream_t stream)
+{
+    int rc = check_world(w);
+    if (rc != TECTO_OK) return rc;
+    if (P < 1 || P > kPlates) {
+        set_error("tecto_world_init_synthetic_device: plate count must be 1..255");
+        return TECTO_ERR_INVALID;
+    }
+    if ((rc = bind_device(w)) != TECTO_OK) return rc;
+    std::vector<float> sx, sy;
+    std::vector<tecto_plate> pl;
+    gen_seeds(w->W, w->H, P, velRange, genSeed, sx, sy, pl);
+    cudaStream_t st = (cudaStream_t)stream;
+    const WorldDev &d = w->dev;
+    w->iteration = 0;
+    TECTO_CUDA(cudaMemsetAsync(w->arena, 0, w->arena_bytes, st));
+    // the seed coordinates ride in the (just cleared) split-path scratch until the kernel ran
+    float *dsx = d.s1, *dsy = d.s1 + kPlates;
+    TECTO_CUDA(cudaMemcpyAsync(dsx, sx.data(), P * sizeof(float), cudaMemcpyHostToDevice, st));
+    TECTO_CUDA(cudaMemcpyAsync(dsy, sy.data(), P * sizeof(float), cudaMemcpyHostToDevice, st));
+    TECTO_CUDA(cudaMemcpyAsync(d.plates, pl.data(), sizeof(tecto_plate) * kPlates, cudaMemcpyHostToDevice, st));
+    Control c{};
+    c.seed = w->seed;
+    TECTO_CUDA(cudaMemcpyAsync(d.ctl, &c, sizeof(c), cudaMemcpyHostToDevice, st));
+    if (w->N < 2 * (size_t)kPlates) {  // too small to borrow the scratch: generate on the host
+        TECTO_CUDA(cudaStreamSynchronize(st));
+        return tecto_world_init_synthetic(w, P, velRange, genSeed, stream);
+    }
+    k_generate<<<(unsigned)((w->N + 255) / 256), 256, 0, st>>>(d.h[w->cur_h], d.id[w->cur_id], w->W, w->H, P,
+                                                             dsx, dsy, genSeed);
+    TECTO_CUDA(cudaGetLastError());
+    TECTO_CUDA(cudaMemsetAsync(d.s1, 0, 2 * kPlates * sizeof(float), st));
+    TECTO_CUDA(cudaStreamSynchronize(st));
+    return TECTO_OK;
+}
+
+int tecto_generate_world_host(int W, int H, int P, float velRange, uint64_t genSeed, float *height_out,
+                              uint8_t *id_out, tecto_plate *plates_out)
+{
+    if (W < 1 || H < 1 || P < 1 || P > kPlates) {
+        set_error("tecto_generate_world_host: invalid size or plate count (1..255)");
+        return TECTO_ERR_INVALID;
+    }
+    std::vector<float> sx, sy;
+    std::vector<tecto_plate> pl;
+    gen_seeds(W, H, P, velRange, genSeed, sx, sy, pl);
     if (plates_out) std::memcpy(plates_out, pl.data(), sizeof(tecto_plate) * kPlates);
     const float fW = (float)W, fH = (float)H;
 #pragma omp parallel for schedule(static)
@@ -344,6 +455,7 @@ int tecto_generate_world_host(int W, int H, int P, float velRange, uint64_t genS
     return TECTO_OK;
 }
 
+
 int tecto_world_init_synthetic(tecto_world *w, int P, float velRange, uint64_t genSeed,
                                tecto_stream_t stream)
 {
@@ -356,19 +468,16 @@ int tecto_world_init_synthetic(tecto_world *w, int P, float velRange, uint64_t g
     rc = tecto_generate_world_host(w->W, w->H, P, velRange, genSeed, h.data(), id.data(), pl.data());
     if (rc != TECTO_OK) return rc;
     cudaStream_t st = (cudaStream_t)stream;
-    drop_graphs(w);
-    w->cur_h = w->cur_wsf = w->cur_id = 0;
-    w->sort_final = 0;
-    w->iteration = 0;
     const size_t N = w->N;
+    const WorldDev &d = w->dev;
+    w->iteration = 0;
     TECTO_CUDA(cudaMemsetAsync(w->arena, 0, w->arena_bytes, st));
-    TECTO_CUDA(cudaMemcpyAsync(w->b.h[0], h.data(), N * 4, cudaMemcpyHostToDevice, st));
-    TECTO_CUDA(cudaMemcpyAsync(w->b.id[0], id.data(), N, cudaMemcpyHostToDevice, st));
-    TECTO_CUDA(cudaMemcpyAsync(w->b.plates, pl.data(), sizeof(tecto_plate) * kPlates,
-                               cudaMemcpyHostToDevice, st));
+    TECTO_CUDA(cudaMemcpyAsync(d.h[w->cur_h], h.data(), N * 4, cudaMemcpyHostToDevice, st));
+    TECTO_CUDA(cudaMemcpyAsync(d.id[w->cur_id], id.data(), N, cudaMemcpyHostToDevice, st));
+    TECTO_CUDA(cudaMemcpyAsync(d.plates, pl.data(), sizeof(tecto_plate) * kPlates, cudaMemcpyHostToDevice, st));
     Control c{};
     c.seed = w->seed;
-    TECTO_CUDA(cudaMemcpyAsync(w->b.ctl, &c, sizeof(c), cudaMemcpyHostToDevice, st));
+    TECTO_CUDA(cudaMemcpyAsync(d.ctl, &c, sizeof(c), cudaMemcpyHostToDevice, st));
     TECTO_CUDA(cudaStreamSynchronize(st));
     return TECTO_OK;
 }
@@ -381,7 +490,7 @@ int tecto_world_field(tecto_world *w, int field, void **device_ptr, size_t *byte
     size_t n;
     field_info(w, field, &p, &n);
     if (!p) {
-        set_error("unknown field");
+        set_error("unknown field (or sort output of a world never stepped alone)");
         return TECTO_ERR_INVALID;
     }
     if (device_ptr) *device_ptr = p;
@@ -432,7 +541,7 @@ int tecto_world_set_plates(tecto_world *w, const tecto_plate *plates, int count,
     if (!plates || count < 0 || count > kPlates) return TECTO_ERR_INVALID;
     if ((rc = bind_device(w)) != TECTO_OK) return rc;
     cudaStream_t st = (cudaStream_t)stream;
-    TECTO_CUDA(cudaMemcpyAsync(w->b.plates, plates, sizeof(tecto_plate) * count, cudaMemcpyHostToDevice, st));
+    TECTO_CUDA(cudaMemcpyAsync(w->dev.plates, plates, sizeof(tecto_plate) * count, cudaMemcpyHostToDevice, st));
     TECTO_CUDA(cudaStreamSynchronize(st));
     return TECTO_OK;
 }
@@ -444,7 +553,7 @@ int tecto_world_get_plates(tecto_world *w, tecto_plate *plates, int count, tecto
     if (!plates || count < 0 || count > kPlates) return TECTO_ERR_INVALID;
     if ((rc = bind_device(w)) != TECTO_OK) return rc;
     cudaStream_t st = (cudaStream_t)stream;
-    TECTO_CUDA(cudaMemcpyAsync(plates, w->b.plates, sizeof(tecto_plate) * count, cudaMemcpyDeviceToHost, st));
+    TECTO_CUDA(cudaMemcpyAsync(plates, w->dev.plates, sizeof(tecto_plate) * count, cudaMemcpyDeviceToHost, st));
     TECTO_CUDA(cudaStreamSynchronize(st));
     return TECTO_OK;
 }
@@ -456,7 +565,7 @@ int tecto_world_set_iteration(tecto_world *w, uint32_t iteration)
     if ((rc = bind_device(w)) != TECTO_OK) return rc;
     TECTO_CUDA(cudaDeviceSynchronize());
     w->iteration = iteration;
-    TECTO_CUDA(cudaMemcpy(&w->b.ctl->iteration, &iteration, 4, cudaMemcpyHostToDevice));
+    TECTO_CUDA(cudaMemcpy(&w->dev.ctl->iteration, &iteration, 4, cudaMemcpyHostToDevice));
     return TECTO_OK;
 }
 
@@ -469,54 +578,70 @@ int tecto_world_get_iteration(const tecto_world *w, uint32_t *iteration)
     return TECTO_OK;
 }
 
+// Phase entry points: each enqueues one phase of the world's own batch of one.
+#define TECTO_PHASE_PROLOGUE                               \
+    int rc = check_world(w);                               \
+    if (rc != TECTO_OK) return rc;                         \
+    if ((rc = bind_device(w)) != TECTO_OK) return rc;      \
+    Batch *b = nullptr;                                    \
+    if ((rc = own_batch(w, &b)) != TECTO_OK) return rc;    \
+    cudaStream_t st = (cudaStream_t)stream;                \
+    const uint64_t before = b->launches;
+
+#define TECTO_PHASE_EPILOGUE           \
+    from_batch(w, *b);                 \
+    w->launches += b->launches - before; \
+    return rc;
+
 int tecto_phase_collide(tecto_world *w, tecto_stream_t stream)
 {
-    int rc = check_world(w);
-    if (rc != TECTO_OK) return rc;
-    if ((rc = bind_device(w)) != TECTO_OK) return rc;
-    return enqueue_collide(w, (cudaStream_t)stream);
+    TECTO_PHASE_PROLOGUE
+    if ((rc = launch_plates(*b, st)) == TECTO_OK && (rc = launch_sort_keys(*b, st)) == TECTO_OK &&
+        (rc = launch_words(*b, st)) == TECTO_OK)
+        rc = launch_type_matrix(*b, st);
+    TECTO_PHASE_EPILOGUE
 }
 
 int tecto_phase_resolve(tecto_world *w, tecto_stream_t stream)
 {
-    int rc = check_world(w);
-    if (rc != TECTO_OK) return rc;
-    if ((rc = bind_device(w)) != TECTO_OK) return rc;
-    return launch_resolve(w, (cudaStream_t)stream);
+    TECTO_PHASE_PROLOGUE
+    rc = launch_resolve(*b, st);
+    TECTO_PHASE_EPILOGUE
 }
 
 int tecto_phase_thermal(tecto_world *w, int iterations, tecto_stream_t stream)
 {
-    int rc = check_world(w);
-    if (rc != TECTO_OK) return rc;
     if (iterations < 0) return TECTO_ERR_INVALID;
-    if ((rc = bind_device(w)) != TECTO_OK) return rc;
-    return launch_thermal(w, iterations, (cudaStream_t)stream);
+    TECTO_PHASE_PROLOGUE
+    rc = launch_thermal(*b, iterations, st);
+    TECTO_PHASE_EPILOGUE
 }
 
 int tecto_phase_hydraulic(tecto_world *w, int iterations, float dt, tecto_stream_t stream)
 {
-    int rc = check_world(w);
-    if (rc != TECTO_OK) return rc;
     if (iterations < 0 || !std::isfinite(dt)) return TECTO_ERR_INVALID;
-    if ((rc = bind_device(w)) != TECTO_OK) return rc;
-    return launch_hydraulic(w, iterations, dt, (cudaStream_t)stream);
+    TECTO_PHASE_PROLOGUE
+    rc = launch_hydraulic(*b, iterations, dt, st);
+    TECTO_PHASE_EPILOGUE
 }
 
 int tecto_phase_finish(tecto_world *w, tecto_stream_t stream)
 {
-    int rc = check_world(w);
-    if (rc != TECTO_OK) return rc;
-    if ((rc = bind_device(w)) != TECTO_OK) return rc;
-    return enqueue_finish(w, (cudaStream_t)stream, ccl_due(w));
+    TECTO_PHASE_PROLOGUE
+    const int period = w->settings.sim.iterationsForCCL > 0 ? w->settings.sim.iterationsForCCL : 1;
+    const bool due = w->iteration % (uint32_t)period == 0;
+    if ((rc = launch_finish(*b, st)) == TECTO_OK &&
+        (!due || (rc = launch_ccl(*b, w->settings.step.cclConnectivity, false, st)) == TECTO_OK) &&
+        (rc = launch_bump_iteration(*b, st)) == TECTO_OK)
+        w->iteration += 1;
+    TECTO_PHASE_EPILOGUE
 }
 
 int tecto_phase_ccl(tecto_world *w, int connectivity, tecto_stream_t stream)
 {
-    int rc = check_world(w);
-    if (rc != TECTO_OK) return rc;
-    if ((rc = bind_device(w)) != TECTO_OK) return rc;
-    return launch_ccl(w, connectivity, (cudaStream_t)stream);
+    TECTO_PHASE_PROLOGUE
+    rc = launch_ccl(*b, connectivity, false, st);
+    TECTO_PHASE_EPILOGUE
 }
 
 int tecto_world_step(tecto_world *w, int nSteps, tecto_stream_t stream)
@@ -525,48 +650,9 @@ int tecto_world_step(tecto_world *w, int nSteps, tecto_stream_t stream)
     if (rc != TECTO_OK) return rc;
     if (nSteps < 0) return TECTO_ERR_INVALID;
     if ((rc = bind_device(w)) != TECTO_OK) return rc;
-    cudaStream_t st = (cudaStream_t)stream;
-    for (int s = 0; s < nSteps; ++s) {
-        const bool ccl = ccl_due(w);
-        if (st == nullptr) {  // the legacy stream cannot be captured: plain launches
-            if ((rc = enqueue_step(w, st, ccl)) != TECTO_OK) return rc;
-            continue;
-        }
-        const int key = w->cur_h | (w->cur_wsf << 1) | (w->cur_id << 2) | ((ccl ? 1 : 0) << 3);
-        if (!w->graph_valid[key]) {
-            cudaGraph_t g = nullptr;
-            const uint64_t before = w->launches;
-            TECTO_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-            rc = enqueue_step(w, st, ccl);
-            const cudaError_t ce = cudaStreamEndCapture(st, &g);
-            if (rc != TECTO_OK) {
-                if (g) cudaGraphDestroy(g);
-                return rc;
-            }
-            if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
-            cudaGraphExec_t ex = nullptr;
-            const cudaError_t ie = cudaGraphInstantiate(&ex, g, 0);
-            cudaGraphDestroy(g);
-            if (ie != cudaSuccess) return cuda_fail(ie, "cudaGraphInstantiate");
-            w->graphs[key] = ex;
-            w->graph_valid[key] = true;
-            w->graph_end[key][0] = w->cur_h;
-            w->graph_end[key][1] = w->cur_wsf;
-            w->graph_end[key][2] = w->cur_id;
-            w->graph_end[key][3] = w->sort_final;
-            w->graph_launches[key] = w->launches - before;
-            TECTO_CUDA(cudaGraphLaunch(ex, st));
-        } else {
-            TECTO_CUDA(cudaGraphLaunch(w->graphs[key], st));
-            w->cur_h = w->graph_end[key][0];
-            w->cur_wsf = w->graph_end[key][1];
-            w->cur_id = w->graph_end[key][2];
-            w->sort_final = w->graph_end[key][3];
-            w->iteration += 1;
-            w->launches += w->graph_launches[key];
-        }
-    }
-    return TECTO_OK;
+    Batch *b = nullptr;
+    if ((rc = own_batch(w, &b)) != TECTO_OK) return rc;
+    return batch_step(*b, nSteps, (cudaStream_t)stream);  // updates the world's halves and counters
 }
 
 int tecto_world_launch_count(const tecto_world *w, uint64_t *count)
@@ -587,11 +673,12 @@ int tecto_world_check(tecto_world *w, tecto_stream_t stream)
     TECTO_CUDA(cudaStreamSynchronize(st));
     TECTO_CUDA(cudaGetLastError());
     uint32_t err[2] = {0, 0};
-    TECTO_CUDA(cudaMemcpy(&err[0], &w->b.ctl->error, 4, cudaMemcpyDeviceToHost));
-    TECTO_CUDA(cudaMemcpy(&err[1], w->b.sort.error, 4, cudaMemcpyDeviceToHost));
+    TECTO_CUDA(cudaMemcpy(&err[0], &w->dev.ctl->error, 4, cudaMemcpyDeviceToHost));
+    if (w->own && w->own->arena && w->own->sort.error)
+        TECTO_CUDA(cudaMemcpy(&err[1], w->own->sort.error, 4, cudaMemcpyDeviceToHost));
     if (err[0] | err[1]) {
-        cudaMemset(&w->b.ctl->error, 0, 4);
-        cudaMemset(w->b.sort.error, 0, 4);
+        cudaMemset(&w->dev.ctl->error, 0, 4);
+        if (w->own && w->own->sort.error) cudaMemset(w->own->sort.error, 0, 4);
         set_error("a bounded device-side wait gave up");
         return TECTO_ERR_DEVICE_TIMEOUT;
     }

@@ -1,11 +1,16 @@
-// tecto_internal.cuh - world layout in HBM, launch parameters and device helpers shared by the
-// engine's kernels.  Reference paths are relative to MarWo22/master_thesis.
+// tecto_internal.cuh - world and batch layout in HBM, launch parameters and device helpers shared
+// by the engine's kernels.  Reference paths are relative to MarWo22/master_thesis.
+//
+// Every phase runs over a batch: a table of world descriptors plus, per phase, one work list of
+// (world, tile) items, so many uneven worlds advance in one launch per phase.  A world stepped on
+// its own is a batch of one.
 #pragma once
 
 #include <cuda_runtime.h>
 #include <cstddef>
 #include <cstdint>
 #include <string>
+#include <vector>
 
 #include "../../include/tecto.h"
 #include "../../include/tecto_math.h"
@@ -19,6 +24,7 @@ constexpr int kSortTile = 4096;                 // keys per onesweep tile (256 t
 constexpr int kSortThreads = 256;
 constexpr int kSortItems = kSortTile / kSortThreads;
 constexpr int kMaxSortPasses = 4;               // 32-bit keys, 8-bit digits
+constexpr int kMaxBatchWorlds = 1024;           // worlds per batch (world lookup table in smem)
 
 // Status word of the decoupled look-back: 2 flag bits + 30 value bits.
 constexpr uint32_t kFlagAggregate = 1u << 30;
@@ -26,7 +32,7 @@ constexpr uint32_t kFlagPrefix = 2u << 30;
 constexpr uint32_t kValueMask = (1u << 30) - 1u;
 constexpr uint32_t kSpinLimit = 1u << 24;       // bounded waits: give up, flag, carry on
 
-// Device error flag bits (control block).
+// Device error flag bits.
 constexpr uint32_t kErrLookbackTimeout = 1u;
 
 // Per-pair collision evidence, CollisionTypeCounts field order
@@ -36,15 +42,20 @@ struct PairCounts {
                // subductionsBOceanic, continental
 };
 
-// Small device-resident control block; kernels read the step counter from here so that a
-// captured graph replays correctly step after step.
+// Per-world device control block; kernels read the step counter from here so that a captured
+// graph replays correctly step after step.
 struct Control {
     uint32_t iteration;     // PlateTectonicSim::m_iterations
     uint32_t seed;          // PlateTectonicSim::m_seed
     uint32_t error;         // kErr* bits
-    uint32_t acc_count;     // entries in the accretion target list this step
-    uint32_t tile_counter[kMaxSortPasses];  // onesweep dynamic tile ids, one per pass
-    uint32_t pad[8];
+    uint32_t acc_count;     // entries in this world's accretion list for the current step
+    uint32_t pad[12];
+};
+
+// Per-batch device control block.
+struct BatchCtl {
+    uint32_t error;
+    uint32_t pad[15];
 };
 
 // Scratch of the radix sort (histograms, look-back status).  Sizes in tecto_sort_scratch_bytes.
@@ -57,22 +68,23 @@ struct SortScratch {
     int tiles;
 };
 
-// Device buffers of one world.  Structure of arrays, one cudaMalloc'd arena.
-struct WorldBuffers {
+// Device descriptor of one world (one cudaMalloc'd arena per world, structure of arrays).
+struct WorldDev {
+    int W, H;
+    uint32_t N;
+    uint32_t vbase;         // first virtual cell index of this world in its batch
     float *h[2];            // height, ping-pong
     float *w[2];            // water
     float *s[2];            // sediment
     float4 *flux[2];        // outflow flux (left, +y, right, -y)
     uint8_t *id[2];         // plate ids
     uint32_t *word;         // packed arrivals per destination cell
-    uint32_t *keys[2];      // sort ping-pong
-    uint32_t *vals[2];
     uint32_t *labels;       // CCL labels
     float *rain;            // this step's rain increment per cell (constant over sub-iterations)
     float2 *vel;            // water velocity, split hydraulic path only
     float *s1;              // sediment before transport, split hydraulic path only
     unsigned long long *acc;  // accretion marks: ((dest + 1) << 8) | (255 - owner), atomicMax
-    uint32_t *acc_list;     // cells with a mark this step
+    uint32_t *acc_list;     // cells holding a mark this step (count in ctl->acc_count)
     uint8_t *acc_u8;        // decoded marks of the last step (download only)
     uint8_t *type_bitmap;   // [kPairs]
     uint32_t *div_bitmap;   // [kDivWords]
@@ -81,7 +93,42 @@ struct WorldBuffers {
     tecto_plate *plates;    // [kPlates]
     int2 *off;              // [kPlates + 1] this step's integer displacement per plate
     Control *ctl;
-    SortScratch sort;
+};
+
+// Phase work lists.
+enum TileKind { TK_RESOLVE = 0, TK_THERMAL, TK_HYDRO, TK_CCL, TK_COUNT };
+
+// One batch: members, their device table, work lists and the batch-level buffers.
+struct Batch {
+    std::vector<tecto_world *> members;
+    tecto_settings settings{};
+    bool has_settings = false;
+    int device = 0;
+    int cur_h = 0, cur_wsf = 0, cur_id = 0;  // aligned ping-pong halves of every member
+    int sort_final = 0;
+    size_t total = 0;                        // sum of member cells
+    int hydro_variant = 0;                   // tile variant the TK_HYDRO list was built for
+    uint64_t launches = 0;
+    bool dirty = true;                       // tables must be rebuilt before the next launch
+    // device tables
+    WorldDev *d_worlds = nullptr;
+    uint32_t *d_vbase = nullptr;             // [n + 1] ascending virtual bases, last = total
+    uint2 *d_tiles[TK_COUNT] = {};           // (world, ty << 16 | tx)
+    int ntiles[TK_COUNT] = {};
+    void *table_arena = nullptr;
+    size_t table_bytes = 0;
+    // batch-level buffers, sized for `capacity` cells
+    size_t capacity = 0;
+    void *arena = nullptr;
+    uint32_t *keys[2] = {};
+    uint32_t *vals[2] = {};
+    BatchCtl *bctl = nullptr;
+    SortScratch sort{};
+    // graphs of one step keyed by (cur_h, cur_wsf, cur_id, ccl)
+    cudaGraphExec_t graphs[16] = {};
+    bool graph_valid[16] = {};
+    int graph_end[16][4] = {};
+    uint64_t graph_launches[16] = {};
 };
 
 }  // namespace tecto
@@ -94,16 +141,16 @@ struct tecto_world {
     uint32_t seed = 0;
     uint32_t iteration = 0;        // host mirror of ctl->iteration
     int cur_h = 0, cur_wsf = 0, cur_id = 0;  // which ping-pong half holds the state
-    int sort_final = 0;            // which keys/vals half holds the last sorted result
-    uint64_t launches = 0;         // kernels enqueued (graph replays count their captured kernels)
+    uint64_t launches = 0;         // kernels enqueued for this world
     void *arena = nullptr;
     size_t arena_bytes = 0;
-    tecto::WorldBuffers b{};
-    // CUDA graphs of one step, keyed by (cur_h, cur_wsf, cur_id, ccl)
-    cudaGraphExec_t graphs[16] = {};
-    bool graph_valid[16] = {};
-    int graph_end[16][4] = {};     // cur_h, cur_wsf, cur_id, sort_final after the graph's step
-    uint64_t graph_launches[16] = {};
+    tecto::WorldDev dev{};         // host copy of the device descriptor
+    tecto::Batch *own = nullptr;   // private batch of one, for stepping alone
+    tecto::Batch *in_batch = nullptr;  // the batch it currently belongs to (own or public)
+};
+
+struct tecto_batch {
+    tecto::Batch b;
 };
 
 namespace tecto {
@@ -149,27 +196,61 @@ __host__ __device__ __forceinline__ uint32_t tri_index(uint32_t i, uint32_t j)
     return i * (2u * kPlates - i - 1u) / 2u + (j - i - 1u);
 }
 
-// ---- phase launchers (each enqueues on `st`) ----------------------------------------------
-int launch_plates(tecto_world *w, cudaStream_t st);
-int launch_sort_keys(tecto_world *w, cudaStream_t st);
-int launch_words(tecto_world *w, cudaStream_t st);
-int launch_type_matrix(tecto_world *w, cudaStream_t st);
-int launch_resolve(tecto_world *w, cudaStream_t st);
-int launch_thermal(tecto_world *w, int iterations, cudaStream_t st);
-int launch_hydraulic(tecto_world *w, int iterations, float dt, cudaStream_t st);
-int launch_finish(tecto_world *w, cudaStream_t st);
-int launch_clear_marks(tecto_world *w, cudaStream_t st);
-int launch_bump_iteration(tecto_world *w, cudaStream_t st);
-void gaussian_weights(float sigma, int radius, float *out);
-int launch_ccl(tecto_world *w, int connectivity, cudaStream_t st);
+// The world owning virtual cell v: largest b with vbase[b] <= v (vbase ascending, n entries).
+__device__ __forceinline__ int find_world(const uint32_t *vbase, int n, uint32_t v)
+{
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (vbase[mid] <= v) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
 
-// Radix sort core (k_sort.cu).  If gen_id != nullptr the first pass generates keys (destination
-// cells) and values (source cells) from plate ids and the per-plate displacement `off`;
-// otherwise it reads keys_in/vals_in.  Returns the half (0/1) of keys/vals holding the result.
+__device__ __forceinline__ void tile_of(uint2 t, int *world, int *tx, int *ty)
+{
+    *world = (int)t.x;
+    *tx = (int)(t.y & 0xffffu);
+    *ty = (int)(t.y >> 16);
+}
+
+// ---- batch management (tecto_batch.cu) -----------------------------------------------------
+int batch_prepare(Batch &b, cudaStream_t st);        // (re)build tables and buffers if dirty
+int batch_enqueue_step(Batch &b, cudaStream_t st, int ccl);  // 0 none, 1 all, 2 where due
+int batch_step(Batch &b, int nsteps, cudaStream_t st);
+int batch_step_graph(Batch &b, int nsteps, cudaStream_t st, bool use_graph);
+void batch_release(Batch &b);
+int batch_join(Batch &b, tecto_world *w, cudaStream_t st);
+int batch_leave(Batch &b, tecto_world *w);
+int tile_extent(int kind, int variant, int *tx, int *ty);
+
+// ---- phase launchers (each enqueues on `st` for every member of the batch) -----------------
+int launch_plates(Batch &b, cudaStream_t st);
+int launch_sort_keys(Batch &b, cudaStream_t st);
+int launch_words(Batch &b, cudaStream_t st);
+int launch_type_matrix(Batch &b, cudaStream_t st);
+int launch_resolve(Batch &b, cudaStream_t st);
+int launch_thermal(Batch &b, int iterations, cudaStream_t st);
+int launch_hydraulic(Batch &b, int iterations, float dt, cudaStream_t st);
+int launch_finish(Batch &b, cudaStream_t st);
+int launch_clear_marks(Batch &b, cudaStream_t st);
+int launch_bump_iteration(Batch &b, cudaStream_t st);
+// due_only: skip worlds whose step counter is not a multiple of iterationsForCCL
+int launch_ccl(Batch &b, int connectivity, bool due_only, cudaStream_t st);
+void gaussian_weights(float sigma, int radius, float *out);
+int ensure_kernel_attributes();
+int hydro_variant_for(const tecto_settings &s);
+
+// Radix sort core (k_sort.cu).  If worlds != nullptr the first pass generates the keys (the
+// batch-virtual destination cell of every virtual cell) and values (the virtual source cell)
+// from each world's plate ids and per-plate displacement; otherwise it reads keys_in/vals_in.
+// Returns the half (0/1) of keys/vals holding the result.
 struct SortArgs {
-    const uint8_t *gen_id;
-    const int2 *gen_off;
-    int W, H;
+    const WorldDev *worlds;
+    const uint32_t *vbase;
+    int nworlds;
+    int cur_id;
     const uint32_t *keys_in;
     const uint32_t *vals_in;
     uint32_t *keys[2];

@@ -1,0 +1,318 @@
+// tecto_server.cu - continuous batching of world-generation requests (host runtime).
+//
+// The reference runs one interactive world (PlateTectonicSim driven by the GUI loop,
+// src/main.cpp:122-161); serving many worlds is this engine's own layer.  Every tick advances all
+// admitted worlds one step as one batch (one launch per phase); waiting requests are admitted
+// first-come first-served whenever their footprint fits the HBM budget; finished worlds leave the
+// batch at once so that newcomers join while others are mid-flight.  World state stays resident
+// in HBM from admission to completion.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <deque>
+#include <new>
+#include <thread>
+#include <vector>
+
+#include "tecto_internal.cuh"
+
+namespace tecto {
+size_t world_footprint(int W, int H);
+int batch_step_graph(Batch &b, int nsteps, cudaStream_t st, bool use_graph);
+}  // namespace tecto
+
+using namespace tecto;
+
+struct tecto_server {
+    tecto_settings settings{};
+    size_t budget = 0;
+    int max_worlds = 0;
+    bool dry = false;
+    double dry_cost = 2e-4;  // seconds per tick per million active cells
+    tecto_batch *batch = nullptr;
+};
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Live {
+    int idx;
+    tecto_world *world;
+    size_t bytes;
+    size_t cells;
+    int steps_left;
+};
+
+double percentile(std::vector<double> v, double q)
+{
+    if (v.empty()) return 0.0;
+    std::sort(v.begin(), v.end());
+    const double pos = q * (double)(v.size() - 1);
+    const size_t lo = (size_t)std::floor(pos), hi = (size_t)std::ceil(pos);
+    return v[lo] + (v[hi] - v[lo]) * (pos - (double)lo);
+}
+
+void finish_stats(const tecto_request *req, int n, const tecto_request_result *res, double wall,
+                  int ticks, int max_active, double peak, tecto_server_stats *stats)
+{
+    if (!stats) return;
+    std::vector<double> lat;
+    tecto_server_stats s{};
+    for (int i = 0; i < n; ++i) {
+        if (res[i].status == TECTO_OK) {
+            ++s.completed;
+            lat.push_back(res[i].finish_s - res[i].arrival_s);
+            s.cell_updates += (double)req[i].width * (double)req[i].height * (double)req[i].steps;
+        } else if (res[i].status == TECTO_ERR_BUDGET) {
+            ++s.rejected;
+        }
+    }
+    s.wall_s = wall;
+    s.ticks = ticks;
+    s.max_active = max_active;
+    s.peak_bytes = peak;
+    s.cell_updates_per_s = wall > 0 ? s.cell_updates / wall : 0.0;
+    s.latency_p50_s = percentile(lat, 0.50);
+    s.latency_p99_s = percentile(lat, 0.99);
+    double sum = 0;
+    for (double x : lat) sum += x;
+    s.latency_mean_s = lat.empty() ? 0.0 : sum / (double)lat.size();
+    *stats = s;
+}
+
+int make_world(tecto_server *sv, const tecto_request &r, cudaStream_t st, tecto_world **out)
+{
+    int rc = tecto_world_create(&sv->settings, r.width, r.height, r.worldSeed, out);
+    if (rc != TECTO_OK) return rc;
+    rc = tecto_world_init_synthetic_device(*out, r.plates, r.velRange, r.genSeed, (tecto_stream_t)st);
+    if (rc != TECTO_OK) {
+        tecto_world_destroy(*out);
+        *out = nullptr;
+    }
+    return rc;
+}
+
+float checksum(tecto_world *w, cudaStream_t st)
+{
+    std::vector<float> h(w->N);
+    if (tecto_world_download(w, TECTO_FIELD_HEIGHT, h.data(), h.size() * 4, (tecto_stream_t)st) != TECTO_OK)
+        return NAN;
+    double s = 0;
+    for (float v : h) s += v;
+    return (float)s;
+}
+
+bool valid_request(const tecto_request &r)
+{
+    return r.width >= 1 && r.height >= 1 && r.plates >= 1 && r.plates <= kPlates && r.steps >= 0 &&
+           (size_t)r.width * (size_t)r.height <= ((size_t)1 << 30);
+}
+
+}  // namespace
+
+extern "C" {
+
+int tecto_server_create(const tecto_settings *settings, size_t budget_bytes, int max_worlds, int flags,
+                        tecto_server **out)
+{
+    if (!settings || !out || budget_bytes == 0) return TECTO_ERR_INVALID;
+    tecto_server *sv = new (std::nothrow) tecto_server();
+    if (!sv) return TECTO_ERR_OOM;
+    sv->settings = *settings;
+    sv->budget = budget_bytes;
+    sv->max_worlds = (max_worlds <= 0 || max_worlds > kMaxBatchWorlds) ? kMaxBatchWorlds : max_worlds;
+    sv->dry = (flags & TECTO_SERVER_DRY_RUN) != 0;
+    *out = sv;
+    return TECTO_OK;
+}
+
+int tecto_server_destroy(tecto_server *sv)
+{
+    if (!sv) return TECTO_OK;
+    if (sv->batch) tecto_batch_destroy(sv->batch);
+    delete sv;
+    return TECTO_OK;
+}
+
+int tecto_server_set_dry_cost(tecto_server *sv, double s)
+{
+    if (!sv || !(s >= 0)) return TECTO_ERR_INVALID;
+    sv->dry_cost = s;
+    return TECTO_OK;
+}
+
+int tecto_server_run_trace(tecto_server *sv, const tecto_request *req, int n, tecto_stream_t stream,
+                           tecto_request_result *res, tecto_server_stats *stats)
+{
+    if (!sv || (n > 0 && (!req || !res))) return TECTO_ERR_INVALID;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (!sv->dry && !sv->batch) {
+        const int rc = tecto_batch_create(&sv->batch);
+        if (rc != TECTO_OK) return rc;
+    }
+    // arrival order (stable on ties)
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) {
+        order[i] = i;
+        res[i] = tecto_request_result{TECTO_OK, req[i].arrival_s, -1.0, -1.0, 0.0f};
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return req[a].arrival_s < req[b].arrival_s; });
+    std::deque<int> waiting;
+    std::vector<Live> live;
+    size_t used = 0;
+    double peak = 0, vclock = 0;  // vclock: simulated time in dry-run mode
+    int next = 0, ticks = 0, max_active = 0, done = 0;
+    const auto t0 = Clock::now();
+    auto now = [&]() {
+        return sv->dry ? vclock : std::chrono::duration<double>(Clock::now() - t0).count();
+    };
+    int rc = TECTO_OK;
+    while (done < n) {
+        double t = now();
+        while (next < n && req[order[next]].arrival_s <= t) waiting.push_back(order[next++]);
+        // admission: first come first served against the budget
+        bool changed = false;
+        while (!waiting.empty()) {
+            const int i = waiting.front();
+            const tecto_request &r = req[i];
+            if (!valid_request(r)) {
+                res[i].status = TECTO_ERR_INVALID;
+                waiting.pop_front();
+                ++done;
+                continue;
+            }
+            const size_t bytes = world_footprint(r.width, r.height);
+            if (bytes > sv->budget) {  // can never fit
+                res[i].status = TECTO_ERR_BUDGET;
+                waiting.pop_front();
+                ++done;
+                continue;
+            }
+            if (used + bytes > sv->budget || (int)live.size() >= sv->max_worlds) break;
+            Live L{i, nullptr, bytes, (size_t)r.width * (size_t)r.height, r.steps};
+            if (!sv->dry) {
+                if ((rc = make_world(sv, r, st, &L.world)) != TECTO_OK) return rc;
+                if ((rc = tecto_batch_add(sv->batch, L.world, stream)) != TECTO_OK) return rc;
+            }
+            used += bytes;
+            peak = std::max(peak, (double)used);
+            res[i].admit_s = now();
+            live.push_back(L);
+            waiting.pop_front();
+            changed = true;
+        }
+        // retire zero-step requests immediately
+        for (size_t k = 0; k < live.size();) {
+            if (live[k].steps_left > 0) { ++k; continue; }
+            const int i = live[k].idx;
+            if (!sv->dry) {
+                res[i].height_checksum = checksum(live[k].world, st);
+                tecto_batch_remove(sv->batch, live[k].world);
+                tecto_world_destroy(live[k].world);
+            }
+            res[i].finish_s = now();
+            used -= live[k].bytes;
+            live.erase(live.begin() + (long)k);
+            ++done;
+            changed = true;
+        }
+        if (live.empty()) {
+            if (next < n && done < n) {  // idle until the next arrival
+                const double wait = req[order[next]].arrival_s - now();
+                if (sv->dry) vclock += std::max(wait, 0.0);
+                else if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(wait));
+            }
+            continue;
+        }
+        max_active = std::max(max_active, (int)live.size());
+        // one tick: every live world advances one step
+        if (sv->dry) {
+            size_t cells = 0;
+            for (const Live &L : live) cells += L.cells;
+            vclock += sv->dry_cost * (double)cells / 1e6;
+        } else {
+            // graphs pay off once the membership is stable; right after a change launch directly
+            rc = batch_step_graph(sv->batch->b, 1, st, !changed);
+            if (rc != TECTO_OK) return rc;
+            TECTO_CUDA(cudaStreamSynchronize(st));
+        }
+        ++ticks;
+        for (size_t k = 0; k < live.size();) {
+            if (--live[k].steps_left > 0) { ++k; continue; }
+            const int i = live[k].idx;
+            if (!sv->dry) {
+                res[i].height_checksum = checksum(live[k].world, st);
+                tecto_batch_remove(sv->batch, live[k].world);
+                tecto_world_destroy(live[k].world);
+            }
+            res[i].finish_s = now();
+            used -= live[k].bytes;
+            live.erase(live.begin() + (long)k);
+            ++done;
+        }
+    }
+    finish_stats(req, n, res, now(), ticks, max_active, peak, stats);
+    if (!sv->dry) return tecto_batch_check(sv->batch, stream);
+    return TECTO_OK;
+}
+
+int tecto_server_run_trace_sequential(tecto_server *sv, const tecto_request *req, int n, tecto_stream_t stream,
+                                      tecto_request_result *res, tecto_server_stats *stats)
+{
+    if (!sv || (n > 0 && (!req || !res))) return TECTO_ERR_INVALID;
+    cudaStream_t st = (cudaStream_t)stream;
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) {
+        order[i] = i;
+        res[i] = tecto_request_result{TECTO_OK, req[i].arrival_s, -1.0, -1.0, 0.0f};
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return req[a].arrival_s < req[b].arrival_s; });
+    double vclock = 0, peak = 0;
+    const auto t0 = Clock::now();
+    auto now = [&]() {
+        return sv->dry ? vclock : std::chrono::duration<double>(Clock::now() - t0).count();
+    };
+    int ticks = 0;
+    for (int k = 0; k < n; ++k) {
+        const int i = order[k];
+        const tecto_request &r = req[i];
+        if (!valid_request(r)) {
+            res[i].status = TECTO_ERR_INVALID;
+            continue;
+        }
+        const size_t bytes = world_footprint(r.width, r.height);
+        if (bytes > sv->budget) {
+            res[i].status = TECTO_ERR_BUDGET;
+            continue;
+        }
+        const double wait = r.arrival_s - now();
+        if (wait > 0) {
+            if (sv->dry) vclock += wait;
+            else std::this_thread::sleep_for(std::chrono::duration<double>(wait));
+        }
+        res[i].admit_s = now();
+        peak = std::max(peak, (double)bytes);
+        if (sv->dry) {
+            vclock += sv->dry_cost * (double)r.width * (double)r.height / 1e6 * (double)r.steps;
+        } else {
+            tecto_world *w = nullptr;
+            int rc = make_world(sv, r, st, &w);
+            if (rc != TECTO_OK) return rc;
+            rc = tecto_world_step(w, r.steps, stream);
+            if (rc == TECTO_OK) rc = tecto_world_check(w, stream);
+            if (rc != TECTO_OK) {
+                tecto_world_destroy(w);
+                return rc;
+            }
+            res[i].height_checksum = checksum(w, st);
+            tecto_world_destroy(w);
+        }
+        ticks += r.steps;
+        res[i].finish_s = now();
+    }
+    finish_stats(req, n, res, now(), ticks, 1, peak, stats);
+    return TECTO_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,134 @@
+"""Batches and the server on the GPU: each world's result is the same alone and in a mixed batch
+(uneven sizes, worlds joining and leaving mid-flight, different ping-pong parity at join), the
+device-side generator equals the host generator, and the server's continuous batching returns the
+same worlds as serving the requests one at a time."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import master_thesis_gb300 as T
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = (T.FIELD_HEIGHT, T.FIELD_WATER, T.FIELD_SEDIMENT, T.FIELD_FLUX, T.FIELD_PLATE_ID, T.FIELD_LABELS,
+          T.FIELD_TYPE_BITMAP, T.FIELD_DIV_BITMAP, T.FIELD_ACCRETION)
+
+SPECS = [(64, 64, 8, 1), (100, 60, 5, 2), (33, 17, 3, 3), (128, 32, 6, 4), (200, 150, 12, 5), (256, 128, 9, 6)]
+
+
+@pytest.fixture(scope="module")
+def stream():
+    torch = pytest.importorskip("torch")
+    assert torch.cuda.is_available(), "a CUDA GPU is required"
+    return torch.cuda.Stream()
+
+
+def settings():
+    s = T.baseline_settings()
+    s.kernel.minCollisionSize = 3
+    s.kernel.collisionTypeUpdateCooldown = 2
+    s.sim.iterationsForCCL = 3
+    return s
+
+
+def make(spec, s):
+    W, H, plates, seed = spec
+    w = T.World(s, W, H, seed=1000 + seed)
+    w.init_synthetic(plates, 1.0, seed)
+    return w
+
+
+def assert_same(a: T.World, b: T.World, msg):
+    for f in FIELDS:
+        np.testing.assert_array_equal(a.download(f), b.download(f), err_msg=f"{msg}: field {f}")
+    np.testing.assert_array_equal(a.plates(), b.plates(), err_msg=f"{msg}: plates")
+    assert a.iteration == b.iteration
+
+
+def test_batch_equals_alone_with_joins_and_leaves(stream):
+    s = settings()
+    alone = [make(sp, s) for sp in SPECS]
+    mixed = [make(sp, s) for sp in SPECS]
+    # a world stepped alone first joins the batch with other ping-pong halves than the batch's
+    mixed[3].step(1, stream)
+    alone[3].step(1, stream)
+    b = T.Batch()
+    for w in mixed[:3]:
+        b.add(w, stream)
+    b.step(2, stream)
+    for w in mixed[3:]:
+        b.add(w, stream)
+    b.step(3, stream)
+    b.remove(mixed[1])
+    b.step(4, stream)  # the first 8 worlds' counters now differ: CCL due per world
+    stream.synchronize()
+    b.check(stream)
+    # steps each world took in the batch (world 3 also took one step alone before joining, which
+    # its alone copy mirrored above)
+    steps = [9, 5, 9, 7, 7, 7]
+    for w, n in zip(alone, steps):
+        w.step(n, stream)
+    stream.synchronize()
+    for i, (a, m) in enumerate(zip(alone, mixed)):
+        assert_same(a, m, f"world {i} {SPECS[i]}")
+    assert b.size() == (5, sum(sp[0] * sp[1] for k, sp in enumerate(SPECS) if k != 1))
+    b.close()
+
+
+def test_batch_matches_oracle(stream):
+    s = settings()
+    worlds = [make(sp, s) for sp in SPECS[:4]]
+    oracles = [O.OracleWorld(s, w.download(T.FIELD_HEIGHT), w.download(T.FIELD_PLATE_ID), w.plates(),
+                             1000 + sp[3]) for w, sp in zip(worlds, SPECS)]
+    b = T.Batch()
+    for w in worlds:
+        b.add(w, stream)
+    b.step(4, stream)
+    stream.synchronize()
+    for w, o in zip(worlds, oracles):
+        o.step(4)
+        np.testing.assert_array_equal(w.download(T.FIELD_PLATE_ID), o.id)
+        np.testing.assert_array_equal(w.download(T.FIELD_LABELS), o.labels)
+        np.testing.assert_array_equal(w.download(T.FIELD_HEIGHT), o.h)
+        np.testing.assert_array_equal(w.download(T.FIELD_WATER), o.w)
+        np.testing.assert_array_equal(w.download(T.FIELD_SEDIMENT), o.s)
+    b.close()
+
+
+@pytest.mark.parametrize("W,H,P", [(64, 64, 8), (300, 170, 12), (1024, 512, 48), (17, 33, 3)])
+def test_device_generator_matches_host(W, H, P):
+    w = T.World(T.baseline_settings(), W, H)
+    w.init_synthetic_device(P, 1.0, 77)
+    h, ids, pl = T.generate_world(W, H, P, 1.0, 77)
+    np.testing.assert_array_equal(w.download(T.FIELD_HEIGHT), h)
+    np.testing.assert_array_equal(w.download(T.FIELD_PLATE_ID), ids)
+    np.testing.assert_array_equal(w.plates(), pl)
+
+
+def test_server_continuous_batching_matches_one_at_a_time(stream):
+    rng = np.random.default_rng(3)
+    sizes = [(32, 32), (64, 64), (96, 64), (128, 128), (48, 96)]
+    reqs = []
+    for i in range(16):
+        W, H = sizes[rng.integers(0, len(sizes))]
+        reqs.append(T.Request(width=W, height=H, plates=int(rng.integers(3, 12)), steps=int(rng.integers(1, 9)),
+                              velRange=1.0, genSeed=100 + i, worldSeed=2000 + i, arrival_s=0.002 * i))
+    budget = 6 * T.world_bytes(128, 128)
+    sv = T.Server(settings(), budget, max_worlds=8)
+    res_c, st_c = sv.run_trace(reqs, stream)
+    res_s, st_s = sv.run_trace_sequential(reqs, stream)
+    assert st_c.completed == st_s.completed == 16
+    assert st_c.peak_bytes <= budget
+    for i, (a, b) in enumerate(zip(res_c, res_s)):
+        assert a.status == b.status == 0
+        assert a.height_checksum == b.height_checksum, f"request {i}"
+    # one request served directly through the plain API
+    q = reqs[5]
+    w = T.World(settings(), q.width, q.height, seed=q.worldSeed)
+    w.init_synthetic_device(q.plates, q.velRange, q.genSeed)
+    w.step(q.steps, stream)
+    stream.synchronize()
+    assert np.float32(w.download(T.FIELD_HEIGHT).astype(np.float64).sum()) == res_c[5].height_checksum
+    sv.close()
