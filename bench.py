@@ -1,24 +1,35 @@
 #!/usr/bin/env python3
-"""Benchmark: cell-updates/s of the plate-tectonics step on GB300.
+"""Benchmark: cell-updates/s of the plate-tectonics step on GB300, batched and served against the
+plain one-world-at-a-time path, with p50/p99 world latency.
 
 One step = advection + sort-based collision + Gaussian uplift + 20 hydraulic + 10 thermal
-sub-iterations + CCL every 10 steps (amortised), on the plain one-world path at 2048 x 2048 with
-32 plates (synthetic seeded world, the benchmark physics).  A cell-update is one cell through one
-step.
+sub-iterations + CCL every 10 steps (amortised), the benchmark physics.  A cell-update is one
+cell through one step.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference] [--quick]
 
-Engine arm: the world stays resident in HBM; K steps replay the captured step graph on one stream,
-timed with CUDA events; `e2e` repeats the measurement through the C ABI with host buffers (upload of
-the world state from pinned memory, step, download of height and plate ids, every step).
+Headline (`value`): the mixed-size batch - 256 worlds, sides log-uniform on 128..1024 (half
+square, half 2:1), plates uniform on 4..32, per-world seeds - advanced together, one launch per
+phase over all worlds, each step one CUDA-graph replay; world state resident in HBM; tile shape
+and sort digit width picked by the autotuner.  Beside it:
+  plain        the same 256 worlds stepped one at a time through the plain path;
+  served       a Poisson trace of world-generation requests (70% 256^2, 25% 1024^2, 5% 4096^2;
+               steps 50..500; plates 8..48; 150 GB budget) at 80% of the plain path's capacity,
+               served with continuous batching and one request at a time: p50/p99 latency,
+               cell-updates/s, and a saturated trace (all requests at t=0) for capacity;
+  plain_2048   one 2048^2 world, 32 plates (plain path; its k_hydro roofline);
+  plain_8192   one 8192^2 world, 64 plates, velocities in [-2, 2], 8-connected CCL every step.
+`e2e` repeats the headline through the C ABI with host buffers: every step uploads each world's
+state from pinned host memory, steps the batch, and downloads heights and plate ids.
 Reference arm: the reference path's CPU implementation (the oracle's C restatement, all host
-threads) on the same configuration.  With N > 1 (torchrun) every rank runs its own world
-(replicas; the step has no cross-world exchange).
+threads) on a bounded sample of the same mixed-size workload.  With N > 1 (torchrun) every rank
+runs its own batch (replicas; worlds never exchange data).
 """
 from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import re
 import statistics
@@ -32,13 +43,15 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-W_DEF = H_DEF = 2048
-PLATES = 32
+N_WORLDS = 256
+SHAPE_SEED = 2026
 # Algorithmic bytes of one hydraulic sub-iteration per cell: read height, water, sediment (12)
 # and flux (16); write the same 28.
 HYDRO_BYTES_PER_CELL = 56
-# Algorithmic bytes of one whole step per cell (phase table in the design doc).
+# Algorithmic bytes of one whole step per cell: advect + sort 25, words 13, resolve + uplift 14,
+# thermal 10 x 8, hydraulic 20 x 56, CCL 5 every 10 steps.
 STEP_BYTES_PER_CELL = 1252.5
+BUDGET_BYTES = 150 * 10**9
 
 
 def measured_peak_hbm():
@@ -51,13 +64,13 @@ def measured_peak_hbm():
     return 6800.0, "fallback 6.8 TB/s"
 
 
-def profiled_traffic():
-    """dram bytes per k_hydro launch from the committed ncu summary, scaled to this workload."""
+def profiled_traffic_per_cell():
+    """dram bytes per cell of one k_hydro launch, from the committed ncu summary (2048^2 capture)."""
     p = ROOT / "profiles" / "k_hydro_2048.md"
     if not p.exists():
         return None
     m = re.search(r"traffic_bytes_per_launch_2048:\s*([0-9.eE+]+)", p.read_text())
-    return float(m.group(1)) if m else None
+    return float(m.group(1)) / (2048 * 2048) if m else None
 
 
 class ClockSampler:
@@ -70,18 +83,19 @@ class ClockSampler:
     def __init__(self, index: int):
         self.index = index
         self.proc = None
+        self.lines = []
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
                  "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            time.sleep(0.3)  # first sample before the timed region
         except OSError:
             self.proc = None
         return self
 
     def __exit__(self, *a):
-        self.lines = []
         if self.proc is not None:
             self.proc.terminate()
             try:
@@ -94,7 +108,7 @@ class ClockSampler:
     def summary(self):
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in getattr(self, "lines", []):
+        for ln in self.lines:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 9:
                 continue
@@ -119,22 +133,55 @@ def dist_setup():
     return ws, rank, local
 
 
-def cpu_rate(W, H, steps_cap, seconds_cap, settings, gen_seed=1):
-    """The oracle (C restatement of the reference step) on all host threads: cell-updates/s."""
+def mixed_worlds(n=N_WORLDS, seed=SHAPE_SEED):
+    """(W, H, plates, gen_seed, world_seed) of the mixed-size batch: side s log-uniform on
+    [128, 1024]; even entries s x s, odd entries s x s/2; plates uniform on 4..32."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        s = int(round(math.exp(rng.uniform(math.log(128), math.log(1024)))))
+        W, H = (s, s) if i % 2 == 0 else (s, max(1, s // 2))
+        out.append((W, H, int(rng.integers(4, 33)), 10_000 + i, 20_000 + i))
+    return out
+
+
+def serve_trace(n, mean_service_s, load, seed=7, saturated=False):
+    """Poisson arrivals at `load` x the plain path's capacity (1 / mean service time)."""
+    import master_thesis_gb300 as T
+
+    rng = np.random.default_rng(seed)
+    lam = load / mean_service_s
+    t = 0.0
+    reqs = []
+    for i in range(n):
+        u = rng.uniform()
+        side = 256 if u < 0.70 else (1024 if u < 0.95 else 4096)
+        steps = int(rng.integers(50, 501))
+        plates = int(rng.integers(8, 49))
+        t += rng.exponential(1.0 / lam)
+        reqs.append(T.Request(width=side, height=side, plates=plates, steps=steps, velRange=1.0,
+                              genSeed=30_000 + i, worldSeed=40_000 + i, arrival_s=0.0 if saturated else t))
+    return reqs, lam
+
+
+def timed_oracle(specs, seconds_cap, settings, start=0):
+    """cell-updates/s of the oracle's step alone (world generation excluded)."""
     import master_thesis_gb300 as T
     import oracle as O
 
-    h, ids, pl = T.generate_world(W, H, PLATES, 1.0, gen_seed)
-    ow = O.OracleWorld(settings, h, ids, pl, 1000)
-    done = 0
-    t0 = time.perf_counter()
-    while done < steps_cap:
+    cells, done, step_s, wall0 = 0, 0, 0.0, time.perf_counter()
+    i = start
+    while time.perf_counter() - wall0 < seconds_cap:
+        W, H, P, gs, wsd = specs[i % len(specs)]
+        h, ids, pl = T.generate_world(W, H, P, 1.0, gs)
+        ow = O.OracleWorld(settings, h, ids, pl, wsd)
+        t1 = time.perf_counter()
         ow.step(1)
+        step_s += time.perf_counter() - t1
+        cells += W * H
         done += 1
-        if time.perf_counter() - t0 > seconds_cap:
-            break
-    dt = time.perf_counter() - t0
-    return W * H * done / dt, done, dt
+        i += 1
+    return cells / step_s, done, step_s, cells
 
 
 def run_reference(args, ws, rank):
@@ -143,23 +190,56 @@ def run_reference(args, ws, rank):
     if rank != 0:
         return
     s = T.baseline_settings()
-    W = H = args.size
+    specs = mixed_worlds()
     cores = os.cpu_count() or 1
-    # warm-up steps, then timed steps, both capped so the arm ends within a few minutes
-    cpu_rate(W, H, max(1, min(args.warmup, 2)), 20.0, s)
-    rate, done, secs = cpu_rate(W, H, args.steps, 150.0, s)
+    # each "step" is a bounded sample of the workload: consecutive worlds of the batch, one step
+    # each, about 1.5 s of CPU work; warm-up samples first
+    timed_oracle(specs, 1.5 * max(1, min(args.warmup, 3)), s)
+    rates, worlds, secs, cells = [], 0, 0.0, 0
+    start = 0
+    for _ in range(args.steps):
+        r, d, st, c = timed_oracle(specs, 1.5, s, start)
+        start += d
+        worlds += d
+        secs += st
+        cells += c
+        rates.append(r)
+    rate = cells / secs
     line = {
         "metric": "cell_updates_per_s", "value": rate, "unit": "cell-updates/s", "n_gpus": args.gpus,
-        "steps": done, "warmup": args.warmup, "ms_per_step": 1e3 * secs / done, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Voronoi world)",
-        "impl": "reference",
-        "config": {"workload": f"plain one-world step, {W}x{H}, {PLATES} plates, benchmark physics",
-                   "grid": [W, H], "plates": PLATES},
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded Voronoi worlds, benchmark physics)", "impl": "reference",
+        "config": {"workload": f"batched mixed-size worlds ({N_WORLDS} worlds, sides log-uniform 128..1024, "
+                               "half square / half 2:1, plates 4..32), benchmark physics",
+                   "worlds": N_WORLDS, "parallelism": "host threads"},
         "cpu_baseline": {"value": rate, "unit": "cell-updates/s", "cores": cores, "kind": "port",
-                         "sample": f"{done} full steps of the {W}x{H} world on {cores} OpenMP threads"},
+                         "sample": f"{worlds} world-steps of the mixed-size batch ({cells} cell-updates, "
+                                   f"{secs:.1f} s of stepping) on {cores} OpenMP threads"},
         "e2e": {"value": rate, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def event_ms(torch, stream, fn):
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    fn()
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def plain_world_rate(T, torch, stream, W, H, plates, vel, steps, settings):
+    """cell-updates/s and ms/step of one world on the plain path (graph replay, resident state)."""
+    w = T.World(settings, W, H, seed=1000)
+    w.init_synthetic_device(plates, vel, 1)
+    w.step(3, stream)
+    stream.synchronize()
+    ms = event_ms(torch, stream, lambda: w.step(steps, stream))
+    w.check(stream)
+    w.close()
+    return W * H * steps / (ms / 1e3), ms / steps
 
 
 def run_engine(args, ws, rank, local):
@@ -173,121 +253,214 @@ def run_engine(args, ws, rank, local):
         import torch.distributed as dist
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    W = H = args.size
-    N = W * H
-    s = T.baseline_settings()
-    world = T.World(s, W, H, seed=1000)
-    world.init_synthetic(PLATES, 1.0, 1 + rank)
-    stream = torch.cuda.Stream()
 
     def barrier():
         if dist is not None:
             dist.barrier()
 
-    # warm-up (captures the step graphs)
-    world.step(args.warmup, stream)
-    stream.synchronize()
-    world.check(stream)
+    def max_over_ranks(x):
+        t = torch.tensor([x], device="cuda", dtype=torch.float64)
+        if dist is not None:
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
 
+    stream = torch.cuda.Stream()
+    s = T.baseline_settings()  # hydraulicTile = sortRadixBits = 0: the autotuner's choice
+    specs = mixed_worlds(seed=SHAPE_SEED + rank)
+    total = sum(W * H for W, H, *_ in specs)
+    tuning = T.autotune(s, [(W, H) for W, H, *_ in specs], stream)
+
+    worlds = []
+    batch = T.Batch()
+    for W, H, P, gs, wsd in specs:
+        w = T.World(s, W, H, seed=wsd)
+        w.init_synthetic_device(P, 1.0, gs)
+        batch.add(w, stream)
+        worlds.append(w)
+    batch.step(args.warmup, stream)
+    stream.synchronize()
+    batch.check(stream)
+
+    launches0 = batch.launches
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    launches0 = world.launches
     with ClockSampler(local) as clk:
         barrier()
         torch.cuda.synchronize()
         e0.record(stream)
-        world.step(args.steps, stream)
+        batch.step(args.steps, stream)
         e1.record(stream)
         torch.cuda.synchronize()
         barrier()
-    ms = e0.elapsed_time(e1)
-    launches = world.launches - launches0
-    world.check(stream)
-    ms_t = torch.tensor([ms], device="cuda")
-    if dist is not None:
-        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
-    ms_max = float(ms_t.item())
-    value = ws * N * args.steps / (ms_max / 1e3)
+    ms = max_over_ranks(e0.elapsed_time(e1))
+    launches = batch.launches - launches0
+    batch.check(stream)
+    value = ws * total * args.steps / (ms / 1e3)
 
-    # dominant kernel: the fused hydraulic sub-iteration, timed alone on the same stream
-    reps = 40
-    world.hydraulic(4, s.step.hydraulicDt, stream)
-    stream.synchronize()
-    h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    h0.record(stream)
-    world.hydraulic(reps, s.step.hydraulicDt, stream)
-    h1.record(stream)
-    stream.synchronize()
-    hydro_ms = h0.elapsed_time(h1) / reps
+    # dominant kernel: the fused hydraulic sub-iteration over the whole batch, on the same stream
+    reps = 20
+    batch.hydraulic(2, s.step.hydraulicDt, stream)
+    hydro_ms = event_ms(torch, stream, lambda: batch.hydraulic(reps, s.step.hydraulicDt, stream)) / reps
     peak, peak_src = measured_peak_hbm()
-    achieved = HYDRO_BYTES_PER_CELL * N / (hydro_ms / 1e3) / 1e9
-    traffic = profiled_traffic()
+    achieved = HYDRO_BYTES_PER_CELL * total / (hydro_ms / 1e3) / 1e9
+    tpc = profiled_traffic_per_cell()
 
-    # e2e through the C ABI with host buffers: upload state, step, download height + ids
-    e2e_steps = max(3, min(args.steps, 10))
-    hosts = {f: torch.from_numpy(world.download(f)).pin_memory() for f in
-             (T.FIELD_HEIGHT, T.FIELD_WATER, T.FIELD_SEDIMENT, T.FIELD_FLUX, T.FIELD_PLATE_ID)}
-    outs = {f: torch.empty_like(hosts[f]).pin_memory() for f in (T.FIELD_HEIGHT, T.FIELD_PLATE_ID)}
+    # e2e through the C ABI with host buffers: upload every world's state, step, download
+    # heights and plate ids
     L = T.lib()
     sp = stream.cuda_stream
+    up_fields = (T.FIELD_HEIGHT, T.FIELD_WATER, T.FIELD_SEDIMENT, T.FIELD_FLUX, T.FIELD_PLATE_ID)
+    down_fields = (T.FIELD_HEIGHT, T.FIELD_PLATE_ID)
+    hosts = [{f: torch.from_numpy(w.download(f)).pin_memory() for f in up_fields} for w in worlds]
+    outs = [{f: torch.empty_like(h[f]).pin_memory() for f in down_fields} for h in hosts]
 
     def e2e_step():
-        for f, t in hosts.items():
-            T.check(L.tecto_world_upload(world.ptr, f, t.data_ptr(), t.numel() * t.element_size(), sp), "upload")
-        world.step(1, stream)
-        for f, t in outs.items():
-            T.check(L.tecto_world_download(world.ptr, f, t.data_ptr(), t.numel() * t.element_size(), sp),
-                    "download")
+        for w, hs in zip(worlds, hosts):
+            for f, t in hs.items():
+                T.check(L.tecto_world_upload(w.ptr, f, t.data_ptr(), t.numel() * t.element_size(), sp), "upload")
+        batch.step(1, stream)
+        for w, os_ in zip(worlds, outs):
+            for f, t in os_.items():
+                T.check(L.tecto_world_download(w.ptr, f, t.data_ptr(), t.numel() * t.element_size(), sp),
+                        "download")
 
     e2e_step()
+    stream.synchronize()
+    e2e_steps = 3
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    x0, x1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    x0.record(stream)
-    for _ in range(e2e_steps):
-        e2e_step()
-    x1.record(stream)
-    torch.cuda.synchronize()
+    e2e_ev = event_ms(torch, stream, lambda: [e2e_step() for _ in range(e2e_steps)])
     wall_ms = (time.perf_counter() - t0) * 1e3
-    e2e_ms = max(x0.elapsed_time(x1), wall_ms)
-    e_t = torch.tensor([e2e_ms], device="cuda")
-    if dist is not None:
-        dist.all_reduce(e_t, op=dist.ReduceOp.MAX)
-    e2e_value = ws * N * e2e_steps / (float(e_t.item()) / 1e3)
-    h2d = sum(t.numel() * t.element_size() for t in hosts.values())
-    d2h = sum(t.numel() * t.element_size() for t in outs.values())
-    world.check(stream)
+    e2e_ms = max_over_ranks(max(e2e_ev, wall_ms))
+    e2e_value = ws * total * e2e_steps / (e2e_ms / 1e3)
+    h2d = sum(t.numel() * t.element_size() for hs in hosts for t in hs.values())
+    d2h = sum(t.numel() * t.element_size() for os_ in outs for t in os_.values())
+    batch.check(stream)
+    del hosts, outs
+    batch.close()
+    for w in worlds:
+        w.close()
+    torch.cuda.empty_cache()
+
+    extras = {}
+    if rank == 0 and not args.quick:
+        extras = engine_extras(args, T, torch, stream, s, specs, total, value)
+    barrier()
 
     if rank == 0:
         cores = os.cpu_count() or 1
-        cpu_value, cpu_steps, cpu_secs = cpu_rate(W, H, 8, 15.0, s)
+        cpu_value, cpu_worlds, cpu_secs, cpu_cells = timed_oracle(specs, 12.0, s)
         line = {
             "metric": "cell_updates_per_s", "value": value, "unit": "cell-updates/s", "n_gpus": ws,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded Voronoi world, benchmark physics)",
-            "config": {"workload": f"plain one-world step, {W}x{H}, {PLATES} plates, benchmark physics "
-                                   "(20 hydraulic + 10 thermal sub-iterations, CCL every 10 steps)",
-                       "grid": [W, H], "plates": PLATES, "parallelism": f"replicas x{ws}",
-                       "l2": "no flush: the world state (~450 MB) exceeds the 126 MB L2 every step"},
+            "data": "synthetic (seeded Voronoi worlds, benchmark physics)",
+            "config": {"workload": f"batched mixed-size worlds: {N_WORLDS} worlds, sides log-uniform 128..1024 "
+                                   "(half square, half 2:1), plates 4..32, per-world seeds; one launch per phase "
+                                   "over all worlds, one CUDA-graph replay per step",
+                       "worlds": N_WORLDS, "cells": total, "parallelism": f"replicas x{ws}",
+                       "tuning": tuning.as_dict(),
+                       "l2": f"no flush: the batch state (~{total * 107 / 1e9:.1f} GB) exceeds the 126 MB L2 "
+                             "many times over every step"},
             "gpu_launches": int(launches),
             "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
-            "roofline": {"bound": "hbm", "kernel": "k_hydro (fused hydraulic sub-iteration)",
+            "roofline": {"bound": "hbm", "kernel": "k_hydro (fused hydraulic sub-iteration, all worlds)",
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": traffic, "peak_source": peak_src,
-                         "ms_per_launch": hydro_ms, "alg_bytes_per_launch": HYDRO_BYTES_PER_CELL * N},
+                         "traffic": None if tpc is None else tpc * total,
+                         "traffic_note": "ncu dram bytes of a 2048^2 launch, scaled per cell",
+                         "peak_source": peak_src, "ms_per_launch": hydro_ms,
+                         "alg_bytes_per_launch": HYDRO_BYTES_PER_CELL * total},
             "step_roofline": {"alg_bytes_per_cell": STEP_BYTES_PER_CELL,
                               "achieved_gbs": STEP_BYTES_PER_CELL * value / ws / 1e9,
                               "frac": STEP_BYTES_PER_CELL * value / ws / 1e9 / peak},
             "cpu_baseline": {"value": cpu_value, "unit": "cell-updates/s", "cores": cores, "kind": "port",
-                             "sample": f"{cpu_steps} full steps of the {W}x{H} world ({cpu_secs:.1f} s)"},
+                             "sample": f"{cpu_worlds} world-steps of the mixed-size batch ({cpu_cells} "
+                                       f"cell-updates, {cpu_secs:.1f} s of stepping)"},
             "clocks": clk.summary(),
+            **extras,
         }
         print(json.dumps(line), flush=True)
-    world.close()
     if dist is not None:
         dist.destroy_process_group()
+
+
+def engine_extras(args, T, torch, stream, s, specs, total, batched_value):
+    peak, _ = measured_peak_hbm()
+    out = {}
+
+    # the same worlds, one at a time through the plain path
+    k = 4
+    plain_ms = 0.0
+    for W, H, P, gs, wsd in specs:
+        w = T.World(s, W, H, seed=wsd)
+        w.init_synthetic_device(P, 1.0, gs)
+        w.step(1, stream)  # captures the world's step graphs
+        stream.synchronize()
+        t0 = time.perf_counter()
+        ev = event_ms(torch, stream, lambda: w.step(k, stream))
+        plain_ms += max(ev, (time.perf_counter() - t0) * 1e3)
+        w.check(stream)
+        w.close()
+    plain_value = total * k / (plain_ms / 1e3)
+    out["plain"] = {"value": plain_value, "unit": "cell-updates/s",
+                    "workload": f"the same {N_WORLDS} worlds stepped one at a time on the plain path "
+                                f"({k} steps each, graph replay)",
+                    "batched_vs_plain": batched_value / plain_value}
+
+    # plain one-world references
+    v2048, ms2048 = plain_world_rate(T, torch, stream, 2048, 2048, 32, 1.0, 20, s)
+    w = T.World(s, 2048, 2048, seed=1000)
+    w.init_synthetic_device(32, 1.0, 1)
+    w.step(1, stream)
+    w.hydraulic(2, s.step.hydraulicDt, stream)
+    hms = event_ms(torch, stream, lambda: w.hydraulic(20, s.step.hydraulicDt, stream)) / 20
+    w.close()
+    ach = HYDRO_BYTES_PER_CELL * 2048 * 2048 / (hms / 1e3) / 1e9
+    out["plain_2048"] = {"value": v2048, "unit": "cell-updates/s", "ms_per_step": ms2048,
+                         "workload": "one 2048x2048 world, 32 plates",
+                         "step_roofline_frac": STEP_BYTES_PER_CELL * v2048 / 1e9 / peak,
+                         "k_hydro": {"ms_per_launch": hms, "achieved_gbs": ach, "frac": ach / peak}}
+    s2 = T.baseline_settings()
+    s2.sim.iterationsForCCL = 1
+    s2.step.cclConnectivity = T.CCL_8
+    v8192, ms8192 = plain_world_rate(T, torch, stream, 8192, 8192, 64, 2.0, 5, s2)
+    out["plain_8192"] = {"value": v8192, "unit": "cell-updates/s", "ms_per_step": ms8192,
+                         "workload": "one 8192x8192 world, 64 plates, velocities in [-2, 2], 8-connected CCL "
+                                     "every step",
+                         "step_roofline_frac": (STEP_BYTES_PER_CELL + 4.5) * v8192 / 1e9 / peak}
+    torch.cuda.empty_cache()
+
+    # serving: plain-path service time per request size sets the arrival rate
+    svc = {}
+    for side in (256, 1024, 4096):
+        v, msps = plain_world_rate(T, torch, stream, side, side, 24, 1.0, 10 if side < 4096 else 4, s)
+        svc[side] = msps / 1e3
+    mean_steps = 275.0
+    mean_service = mean_steps * (0.70 * svc[256] + 0.25 * svc[1024] + 0.05 * svc[4096])
+    n_req = args.serve_requests
+    served = {"plain_step_ms": {str(k): round(v * 1e3, 4) for k, v in svc.items()},
+              "mean_plain_service_s": mean_service, "budget_bytes": BUDGET_BYTES, "requests": n_req}
+    for name, saturated in (("poisson", False), ("saturated", True)):
+        reqs, lam = serve_trace(n_req, mean_service, 0.8, saturated=saturated)
+        sv = T.Server(s, BUDGET_BYTES)
+        res_c, st_c = sv.run_trace(reqs, stream)
+        res_s, st_s = sv.run_trace_sequential(reqs, stream)
+        sv.close()
+        same = all(a.status == b.status == 0 and a.height_checksum == b.height_checksum
+                   for a, b in zip(res_c, res_s))
+        served[name] = {
+            "arrival_rate_per_s": None if saturated else lam,
+            "continuous": {"cell_updates_per_s": st_c.cell_updates_per_s, "p50_s": st_c.latency_p50_s,
+                           "p99_s": st_c.latency_p99_s, "wall_s": st_c.wall_s, "max_active": st_c.max_active,
+                           "peak_bytes": st_c.peak_bytes, "completed": st_c.completed},
+            "one_at_a_time": {"cell_updates_per_s": st_s.cell_updates_per_s, "p50_s": st_s.latency_p50_s,
+                              "p99_s": st_s.latency_p99_s, "wall_s": st_s.wall_s, "completed": st_s.completed},
+            "throughput_ratio": st_c.cell_updates_per_s / max(st_s.cell_updates_per_s, 1e-9),
+            "results_identical": bool(same),
+        }
+    out["served"] = served
+    return out
 
 
 def main():
@@ -296,7 +469,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
-    ap.add_argument("--size", type=int, default=W_DEF)
+    ap.add_argument("--serve-requests", type=int, default=40)
+    ap.add_argument("--quick", action="store_true", help="headline only (no plain/served/large-world lines)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_setup()

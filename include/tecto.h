@@ -35,6 +35,7 @@ extern "C" {
 #define TECTO_ERR_DEVICE_TIMEOUT (-4) /* a bounded device-side wait gave up (error flag set) */
 #define TECTO_ERR_UNSUPPORTED (-5)    /* configuration the engine does not implement */
 #define TECTO_ERR_BUDGET (-6)         /* admission refused: memory budget exhausted */
+#define TECTO_ERR_NOT_FOUND (-7)      /* lookup found no entry (autotuner cache) */
 
 typedef struct CUstream_st *tecto_stream_t; /* same type as cudaStream_t */
 typedef struct tecto_world tecto_world;
@@ -114,7 +115,9 @@ typedef struct tecto_simulation_settings {
 /* CCL connectivity modes. */
 #define TECTO_CCL_4 4
 #define TECTO_CCL_8 8
-#define TECTO_CCL_REF8 9 /* the union set of src/cuda_compute/ccl.cu:90-177 */
+#define TECTO_CCL_REF8 9 /* the union set the reference's kernels build (src/cuda_compute/ccl.cu:
+                            90-177): init's link to the first equal of (tl, t, tr, l), then l and tl
+                            unions on every row and t and tr unions on row 0 */
 
 /* Knobs the reference hard-codes (plate_tectonic_sim.cu:73, :336-363) or does not have. */
 typedef struct tecto_step_settings {
@@ -126,9 +129,9 @@ typedef struct tecto_step_settings {
     float upliftSigma;        /* Gaussian sigma in cells */
     int upliftRadius;         /* taps on each side (<= 8) */
     int cclConnectivity;      /* TECTO_CCL_* */
-    int sortRadixBits;        /* 0 = autotuned; else 6..8 */
-    int hydraulicTile;        /* 0 = default; 1: 64x16/256 threads, 2: 64x32/256, 3: 64x32/512,
-                                 4: 64x32/1024, 5: 64x64/1024 */
+    int sortRadixBits;        /* collision sort digit width 8..11; 0 = autotuner's choice, else 8 */
+    int hydraulicTile;        /* 0 = autotuner's choice, else 4; 1: 64x16/256 threads, 2: 64x32/256,
+                                 3: 64x32/512, 4: 64x32/1024, 5: 64x64/1024 */
     int reserved[6];
 } tecto_step_settings;
 
@@ -301,6 +304,36 @@ int tecto_batch_step(tecto_batch *batch, int nSteps, tecto_stream_t stream);
 int tecto_batch_size(const tecto_batch *batch, int *worlds, size_t *cells);
 int tecto_batch_launch_count(const tecto_batch *batch, uint64_t *count);
 int tecto_batch_check(tecto_batch *batch, tecto_stream_t stream);
+/* Phases over every world of the batch (one launch per sub-iteration): for measurement and
+ * parity tests, like the per-world phase calls above. */
+int tecto_batch_phase_hydraulic(tecto_batch *batch, int iterations, float dt, tecto_stream_t stream);
+int tecto_batch_phase_thermal(tecto_batch *batch, int iterations, tecto_stream_t stream);
+
+/* ---- autotuner ---------------------------------------------------------------------------
+ *
+ * No counterpart in the reference (fixed launch shapes, plate_tectonic_sim.cu).  Times every
+ * hydraulic tile variant (one sub-iteration) and every sort digit width (the collision sort) on
+ * scratch worlds of the given shapes with synthetic content, and returns the fastest of each.
+ * The caller's worlds are not touched.  The choice is cached per device and batch shape class
+ * (total cells and mean world cells, half-octave classes); batches whose settings leave
+ * hydraulicTile / sortRadixBits at 0 use the choice cached for their class, else for the nearest
+ * tuned class on their device, else the defaults (variant 4, 8-bit digits). */
+typedef struct tecto_tuning {
+    int hydraulicTile;       /* chosen variant, 1..5 */
+    int sortRadixBits;       /* chosen digit width, 8..11 */
+    float hydraulic_ms[5];   /* one hydraulic sub-iteration with variant 1..5 */
+    float sort_ms[4];        /* the collision sort with 8..11-bit digits */
+} tecto_tuning;
+int tecto_autotune(const tecto_settings *settings, const int *widths, const int *heights, int count,
+                   tecto_stream_t stream, tecto_tuning *out);
+/* Tune for the batch's current member shapes and apply the choice to this batch. */
+int tecto_batch_autotune(tecto_batch *batch, tecto_stream_t stream, tecto_tuning *out);
+/* Tune for one world's shape and apply the choice to its plain stepping. */
+int tecto_world_autotune(tecto_world *world, tecto_stream_t stream, tecto_tuning *out);
+/* Cache access (no device work): record a choice for a class, look one up, clear the cache. */
+int tecto_autotune_record(int device, size_t total_cells, int worlds, int hydraulicTile, int sortRadixBits);
+int tecto_autotune_lookup(int device, size_t total_cells, int worlds, int *hydraulicTile, int *sortRadixBits);
+int tecto_autotune_clear(void);
 
 /* Device bytes one world of width x height holds, including its share of batch buffers: the
  * admission cost used by the server below. */

@@ -25,6 +25,7 @@ ERRORS = {
     -4: "TECTO_ERR_DEVICE_TIMEOUT",
     -5: "TECTO_ERR_UNSUPPORTED",
     -6: "TECTO_ERR_BUDGET",
+    -7: "TECTO_ERR_NOT_FOUND",
 }
 MAX_PLATES = 255
 NUM_PAIRS = 32385
@@ -169,6 +170,19 @@ class ServerStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class Tuning(C.Structure):
+    """tecto_tuning: the autotuner's choice and the per-candidate timings."""
+    _fields_ = [
+        ("hydraulicTile", C.c_int), ("sortRadixBits", C.c_int),
+        ("hydraulic_ms", C.c_float * 5), ("sort_ms", C.c_float * 4),
+    ]
+
+    def as_dict(self) -> dict:
+        return {"hydraulicTile": self.hydraulicTile, "sortRadixBits": self.sortRadixBits,
+                "hydraulic_ms": [round(x, 4) for x in self.hydraulic_ms],
+                "sort_ms": [round(x, 4) for x in self.sort_ms]}
+
+
 SERVER_DRY_RUN = 1
 
 PLATE_DTYPE = np.dtype(
@@ -227,6 +241,14 @@ def _declare(L: C.CDLL) -> None:
         "tecto_batch_size": ([P, C.POINTER(C.c_int), C.POINTER(C.c_size_t)], C.c_int),
         "tecto_batch_launch_count": ([P, C.POINTER(C.c_uint64)], C.c_int),
         "tecto_batch_check": ([P, P], C.c_int),
+        "tecto_batch_phase_hydraulic": ([P, C.c_int, C.c_float, P], C.c_int),
+        "tecto_batch_phase_thermal": ([P, C.c_int, P], C.c_int),
+        "tecto_autotune": ([C.POINTER(Settings), P, P, C.c_int, P, C.POINTER(Tuning)], C.c_int),
+        "tecto_batch_autotune": ([P, P, C.POINTER(Tuning)], C.c_int),
+        "tecto_world_autotune": ([P, P, C.POINTER(Tuning)], C.c_int),
+        "tecto_autotune_record": ([C.c_int, C.c_size_t, C.c_int, C.c_int, C.c_int], C.c_int),
+        "tecto_autotune_lookup": ([C.c_int, C.c_size_t, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)], C.c_int),
+        "tecto_autotune_clear": ([], C.c_int),
         "tecto_server_create": ([C.POINTER(Settings), C.c_size_t, C.c_int, C.c_int, C.POINTER(P)], C.c_int),
         "tecto_server_destroy": ([P], C.c_int),
         "tecto_server_run_trace": ([P, C.POINTER(Request), C.c_int, P, C.POINTER(RequestResult),
@@ -394,6 +416,11 @@ class World:
     def hydraulic(self, iters: int, dt: float, stream=None):
         check(lib().tecto_phase_hydraulic(self.ptr, iters, dt, _stream(stream)), "tecto_phase_hydraulic")
 
+    def autotune(self, stream=None) -> Tuning:
+        t = Tuning()
+        check(lib().tecto_world_autotune(self.ptr, _stream(stream), C.byref(t)), "tecto_world_autotune")
+        return t
+
     def finish(self, stream=None):
         check(lib().tecto_phase_finish(self.ptr, _stream(stream)), "tecto_phase_finish")
 
@@ -456,6 +483,17 @@ class Batch:
     def check(self, stream=None) -> None:
         check(lib().tecto_batch_check(self.ptr, _stream(stream)), "tecto_batch_check")
 
+    def hydraulic(self, iters: int, dt: float, stream=None) -> None:
+        check(lib().tecto_batch_phase_hydraulic(self.ptr, iters, dt, _stream(stream)), "tecto_batch_phase_hydraulic")
+
+    def thermal(self, iters: int, stream=None) -> None:
+        check(lib().tecto_batch_phase_thermal(self.ptr, iters, _stream(stream)), "tecto_batch_phase_thermal")
+
+    def autotune(self, stream=None) -> Tuning:
+        t = Tuning()
+        check(lib().tecto_batch_autotune(self.ptr, _stream(stream), C.byref(t)), "tecto_batch_autotune")
+        return t
+
     def close(self) -> None:
         if getattr(self, "ptr", None):
             lib().tecto_batch_destroy(self.ptr)
@@ -466,6 +504,34 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def autotune(settings: Settings, shapes, stream=None) -> Tuning:
+    """Tune the hydraulic tile and sort digit width for worlds of these (width, height) shapes."""
+    n = len(shapes)
+    ws = (C.c_int * n)(*[int(w) for w, _ in shapes])
+    hs = (C.c_int * n)(*[int(h) for _, h in shapes])
+    t = Tuning()
+    check(lib().tecto_autotune(C.byref(settings), ws, hs, n, _stream(stream), C.byref(t)), "tecto_autotune")
+    return t
+
+
+def autotune_record(device: int, total_cells: int, worlds: int, hydraulic_tile: int, radix_bits: int) -> None:
+    check(lib().tecto_autotune_record(device, total_cells, worlds, hydraulic_tile, radix_bits), "tecto_autotune_record")
+
+
+def autotune_lookup(device: int, total_cells: int, worlds: int):
+    """(hydraulicTile, sortRadixBits) cached for the class, or None."""
+    h, r = C.c_int(), C.c_int()
+    rc = lib().tecto_autotune_lookup(device, total_cells, worlds, C.byref(h), C.byref(r))
+    if rc == -7:
+        return None
+    check(rc, "tecto_autotune_lookup")
+    return h.value, r.value
+
+
+def autotune_clear() -> None:
+    check(lib().tecto_autotune_clear(), "tecto_autotune_clear")
 
 
 class Server:

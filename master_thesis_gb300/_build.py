@@ -21,6 +21,7 @@ SOURCES = [
     "tecto_api.cu",
     "tecto_batch.cu",
     "tecto_server.cu",
+    "tecto_tune.cu",
     "k_sort.cu",
     "k_sort_noalloc.cu",
     "k_collide.cu",

@@ -193,7 +193,7 @@ int launch_sort_keys(Batch &b, cudaStream_t st)
     const int rc = run_sort(a, b.sort, st, &half);
     if (rc != TECTO_OK) return rc;
     b.sort_final = half;
-    b.launches += 2 + (uint64_t)sort_passes_for(a.key_bits);
+    b.launches += 2 + (uint64_t)b.sort.passes;
     return TECTO_OK;
 }
 

@@ -11,14 +11,34 @@
 // scatters through shared memory so that runs of equal digits leave as contiguous stores.
 // The first pass can generate its keys from plate ids (advection fused into the sort: the key
 // of cell i is getPixelMovements' wrapped destination, plate_tectonics_kernel.cu:248-265).
+//
+// The digit width RB is a template parameter (8..11 bits): wider digits mean fewer passes over
+// the keys but larger per-tile histograms and look-back tables; the autotuner picks per size.
 #include "tecto_internal.cuh"
 
 namespace tecto {
 
 namespace {
 
-constexpr int kRadix = 256;
 constexpr int kWarps = kSortThreads / 32;
+
+template <int RB>
+struct Digits {
+    static constexpr int R = 1 << RB;               // digit values per pass
+    static constexpr int DPT = R / kSortThreads;     // digits owned by each thread of a pass
+    static constexpr uint32_t MASK = (uint32_t)R - 1u;
+    static constexpr int MAX_PASSES = (32 + RB - 1) / RB;
+    static_assert(RB >= 8 && RB <= kMaxRadixBits, "digit width out of range");
+};
+
+// Dynamic shared memory of one pass: per-warp digit counts, per-digit tile start and global
+// base, the staged keys and values, and (key generation) the batch's world bases.
+template <int RB>
+constexpr size_t pass_smem(bool gen)
+{
+    return ((size_t)kWarps * Digits<RB>::R + 2 * (size_t)Digits<RB>::R + 2 * (size_t)kSortTile +
+            (gen ? (size_t)kMaxBatchWorlds + 1 : 0)) * sizeof(uint32_t);
+}
 
 // Batch-virtual destination of virtual cell i: the owning world's getPixelMovements destination
 // (plate_tectonics_kernel.cu:248-265) offset by the world's virtual base.
@@ -57,13 +77,14 @@ __device__ __forceinline__ void st_volatile(uint32_t *p, uint32_t v)
 }
 
 // Digit histograms of all passes in one read of the keys.
-template <bool GEN>
+template <bool GEN, int RB>
 __global__ __launch_bounds__(256) void k_sort_hist(GenArgs g, const uint32_t *keys_in, size_t n,
                                                    int passes, uint32_t *hist)
 {
-    __shared__ uint32_t s_hist[kMaxSortPasses][kRadix];
+    using D = Digits<RB>;
+    __shared__ uint32_t s_hist[D::MAX_PASSES][D::R];
     __shared__ uint32_t s_vbase[GEN ? kMaxBatchWorlds : 1];
-    for (int i = threadIdx.x; i < kMaxSortPasses * kRadix; i += blockDim.x) (&s_hist[0][0])[i] = 0;
+    for (int i = threadIdx.x; i < D::MAX_PASSES * D::R; i += blockDim.x) (&s_hist[0][0])[i] = 0;
     if (GEN) load_vbase(g, s_vbase);
     __syncthreads();
     const unsigned lane = threadIdx.x & 31u;
@@ -76,59 +97,86 @@ __global__ __launch_bounds__(256) void k_sort_hist(GenArgs g, const uint32_t *ke
         uint32_t key = 0;
         if (valid) key = GEN ? gen_key(i, g, s_vbase) : keys_in[i];
         for (int p = 0; p < passes; ++p) {
-            const uint32_t d = valid ? ((key >> (8 * p)) & 0xFFu) : 0x100u;
+            const uint32_t d = valid ? ((key >> (RB * p)) & D::MASK) : (uint32_t)D::R;
             const unsigned peers = __match_any_sync(0xffffffffu, d);
             if (valid && (peers & ((1u << lane) - 1u)) == 0)
                 atomicAdd(&s_hist[p][d], (uint32_t)__popc(peers));
         }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < passes * kRadix; i += blockDim.x) {
+    for (int i = threadIdx.x; i < passes * D::R; i += blockDim.x) {
         const uint32_t v = (&s_hist[0][0])[i];
         if (v) atomicAdd(&hist[i], v);
     }
 }
 
-// Exclusive scan of each pass's 256 digit counts, in place.  One block of 256 threads.
+// Block-wide exclusive scan of one value per thread (256 threads); returns the exclusive prefix
+// and the block total.  s_w holds kWarps words; the call ends with a barrier.
+__device__ __forceinline__ uint32_t block_scan(uint32_t v, uint32_t *s_w, uint32_t *total)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t inc = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += u;
+    }
+    if (lane == 31) s_w[warp] = inc;
+    __syncthreads();
+    uint32_t wb = 0, all = 0;
+#pragma unroll
+    for (int k = 0; k < kWarps; ++k) {
+        const uint32_t x = s_w[k];
+        wb += k < warp ? x : 0u;
+        all += x;
+    }
+    __syncthreads();
+    *total = all;
+    return wb + inc - v;
+}
+
+// Exclusive scan of each pass's digit counts, in place.  One block of 256 threads; thread t owns
+// digits t, t + 256, ... and the chunks of 256 digits are scanned in order.
+template <int RB>
 __global__ void k_sort_scan(uint32_t *hist, int passes)
 {
+    using D = Digits<RB>;
     __shared__ uint32_t s_w[kWarps];
-    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int t = threadIdx.x;
     for (int p = 0; p < passes; ++p) {
-        const uint32_t v = hist[p * kRadix + t];
-        uint32_t inc = v;
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
-            if (lane >= o) inc += u;
+        uint32_t carry = 0;
+        for (int c = 0; c < D::DPT; ++c) {
+            uint32_t *h = hist + (size_t)p * D::R + c * kSortThreads + t;
+            const uint32_t v = *h;
+            uint32_t tot = 0;
+            const uint32_t ex = block_scan(v, s_w, &tot);
+            *h = carry + ex;
+            carry += tot;
         }
-        if (lane == 31) s_w[warp] = inc;
-        __syncthreads();
-        uint32_t wbase = 0;
-        for (int k = 0; k < warp; ++k) wbase += s_w[k];
-        hist[p * kRadix + t] = wbase + inc - v;
-        __syncthreads();
     }
 }
 
 // One onesweep pass.
-template <bool GEN>
+template <bool GEN, int RB>
 __global__ __launch_bounds__(kSortThreads) void k_sort_pass(
     GenArgs g, const uint32_t *keys_in,
     const uint32_t *vals_in, uint32_t *keys_out, uint32_t *vals_out, size_t n, int shift,
     const uint32_t *digit_start, uint32_t *status, uint32_t *tile_counter, uint32_t *error)
 {
-    __shared__ uint32_t s_cnt[kWarps][kRadix];  // per-warp digit counts, then warp offsets
-    __shared__ uint32_t s_start[kRadix];        // tile-local exclusive start per digit
-    __shared__ uint32_t s_base[kRadix];         // global output position of the digit's run
-    __shared__ uint32_t s_keys[kSortTile];
-    __shared__ uint32_t s_vals[kSortTile];
-    __shared__ uint32_t s_vbase[GEN ? kMaxBatchWorlds : 1];
-    __shared__ uint32_t s_wsum[kWarps];
+    using D = Digits<RB>;
+    constexpr int R = D::R, DPT = D::DPT;
+    extern __shared__ __align__(16) uint32_t sm_sort[];
+    uint32_t *s_cnt = sm_sort;                   // [kWarps][R] per-warp counts, then warp offsets
+    uint32_t *s_start = s_cnt + kWarps * R;      // tile-local exclusive start per digit
+    uint32_t *s_base = s_start + R;              // global output position of the digit's run
+    uint32_t *s_keys = s_base + R;
+    uint32_t *s_vals = s_keys + kSortTile;
+    uint32_t *s_vbase = s_vals + kSortTile;      // key generation only
+    __shared__ uint32_t s_w[kWarps];
     __shared__ uint32_t s_tile;
 
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     if (t == 0) s_tile = atomicAdd(tile_counter, 1u);
-    for (int i = t; i < kWarps * kRadix; i += kSortThreads) (&s_cnt[0][0])[i] = 0;
+    for (int i = t; i < kWarps * R; i += kSortThreads) s_cnt[i] = 0;
     if (GEN) load_vbase(g, s_vbase);
     __syncthreads();
     const uint32_t tile = s_tile;
@@ -156,79 +204,102 @@ __global__ __launch_bounds__(kSortThreads) void k_sort_pass(
     // Warp-level ranking: items are visited in element order (item, lane), so the rank of an
     // item among equal digits of its warp preserves input order (stability).
     const unsigned lt = (1u << lane) - 1u;
+    uint32_t *my_cnt = s_cnt + warp * R;
 #pragma unroll
     for (int it = 0; it < kSortItems; ++it) {
         const bool valid = wbase + (size_t)it * 32 + lane < n;
-        const uint32_t d = (k[it] >> shift) & 0xFFu;
+        const uint32_t d = (k[it] >> shift) & D::MASK;
         unsigned peers = __ballot_sync(0xffffffffu, valid);
 #pragma unroll
-        for (int b = 0; b < 8; ++b) {
+        for (int b = 0; b < RB; ++b) {
             const bool bit = (d >> b) & 1u;
             const unsigned bb = __ballot_sync(0xffffffffu, bit);
             peers &= bit ? bb : ~bb;
         }
         uint32_t before = 0;
-        if (valid) before = s_cnt[warp][d];
+        if (valid) before = my_cnt[d];
         __syncwarp();
-        if (valid && (peers & lt) == 0) s_cnt[warp][d] = before + (uint32_t)__popc(peers);
+        if (valid && (peers & lt) == 0) my_cnt[d] = before + (uint32_t)__popc(peers);
         __syncwarp();
         rank[it] = before + (uint32_t)__popc(peers & lt);
     }
     __syncthreads();
 
-    // Per digit (thread t owns digit t): warp offsets and the tile's count of that digit.
-    uint32_t run = 0;
+    // Per owned digit d = t + 256 c: warp offsets and the tile's count of that digit, published
+    // at once so that later tiles can start their look-back.
+    uint32_t run[DPT];
+    uint32_t *my_status = status + (size_t)tile * R;
 #pragma unroll
-    for (int w = 0; w < kWarps; ++w) {
-        const uint32_t c = s_cnt[w][t];
-        s_cnt[w][t] = run;
-        run += c;
-    }
-    // Exclusive scan of the tile counts over digits.
-    uint32_t inc = run;
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
-        if (lane >= o) inc += u;
-    }
-    if (lane == 31) s_wsum[warp] = inc;
-
-    // Decoupled look-back for digit t.
-    uint32_t *my = status + (size_t)tile * kRadix + t;
-    uint32_t prefix = 0;
-    if (tile == 0) {
-        st_volatile(my, kFlagPrefix | run);
-    } else {
-        st_volatile(my, kFlagAggregate | run);
-        int j = (int)tile - 1;
-        uint32_t spins = 0;
-        while (j >= 0) {
-            const uint32_t s = ld_volatile(status + (size_t)j * kRadix + t);
-            if ((s & ~kValueMask) == 0) {
-                if (++spins > kSpinLimit) {  // predecessor never published: flag and give up
-                    atomicOr(error, kErrLookbackTimeout);
-                    break;
-                }
-                continue;
-            }
-            prefix += s & kValueMask;
-            if (s & kFlagPrefix) break;
-            --j;
+    for (int c = 0; c < DPT; ++c) {
+        const int d = t + c * kSortThreads;
+        uint32_t r = 0;
+#pragma unroll
+        for (int w = 0; w < kWarps; ++w) {
+            const uint32_t x = s_cnt[w * R + d];
+            s_cnt[w * R + d] = r;
+            r += x;
         }
-        st_volatile(my, kFlagPrefix | ((prefix + run) & kValueMask));
+        run[c] = r;
+        st_volatile(my_status + d, (tile == 0 ? kFlagPrefix : kFlagAggregate) | r);
     }
-    __syncthreads();
-    uint32_t wb = 0;
-    for (int w = 0; w < warp; ++w) wb += s_wsum[w];
-    s_start[t] = wb + inc - run;
-    s_base[t] = digit_start[t] + prefix;
+    // Tile-local exclusive start of every digit (chunks of 256 digits in order).
+    uint32_t carry = 0;
+#pragma unroll
+    for (int c = 0; c < DPT; ++c) {
+        uint32_t tot = 0;
+        const uint32_t ex = block_scan(run[c], s_w, &tot);
+        s_start[t + c * kSortThreads] = carry + ex;
+        carry += tot;
+    }
+
+    // Decoupled look-back for the owned digits, walked side by side.
+    uint32_t prefix[DPT];
+#pragma unroll
+    for (int c = 0; c < DPT; ++c) prefix[c] = 0;
+    if (tile > 0) {
+        int j[DPT];
+#pragma unroll
+        for (int c = 0; c < DPT; ++c) j[c] = (int)tile - 1;
+        uint32_t spins = 0;
+        bool pending = true;
+        while (pending) {
+            pending = false;
+            bool progressed = false;
+#pragma unroll
+            for (int c = 0; c < DPT; ++c) {
+                if (j[c] < 0) continue;
+                const uint32_t s = ld_volatile(status + (size_t)j[c] * R + t + c * kSortThreads);
+                if ((s & ~kValueMask) == 0) {
+                    pending = true;
+                    continue;
+                }
+                progressed = true;
+                prefix[c] += s & kValueMask;
+                j[c] = (s & kFlagPrefix) ? -1 : j[c] - 1;
+                if (j[c] >= 0) pending = true;
+            }
+            if (pending && !progressed && ++spins > kSpinLimit) {  // a predecessor never published
+                atomicOr(error, kErrLookbackTimeout);
+                break;
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < DPT; ++c)
+            st_volatile(my_status + t + c * kSortThreads, kFlagPrefix | ((prefix[c] + run[c]) & kValueMask));
+    }
+#pragma unroll
+    for (int c = 0; c < DPT; ++c) {
+        const int d = t + c * kSortThreads;
+        s_base[d] = digit_start[d] + prefix[c];
+    }
     __syncthreads();
 
     // Scatter into shared memory in digit order.
 #pragma unroll
     for (int it = 0; it < kSortItems; ++it) {
         if (wbase + (size_t)it * 32 + lane < n) {
-            const uint32_t d = (k[it] >> shift) & 0xFFu;
-            const uint32_t pos = s_start[d] + s_cnt[warp][d] + rank[it];
+            const uint32_t d = (k[it] >> shift) & D::MASK;
+            const uint32_t pos = s_start[d] + my_cnt[d] + rank[it];
             s_keys[pos] = k[it];
             s_vals[pos] = v[it];
         }
@@ -236,18 +307,81 @@ __global__ __launch_bounds__(kSortThreads) void k_sort_pass(
     __syncthreads();
     const size_t rem = n - base;
     const uint32_t tile_n = rem < (size_t)kSortTile ? (uint32_t)rem : (uint32_t)kSortTile;
-    for (uint32_t j = t; j < tile_n; j += kSortThreads) {
-        const uint32_t key = s_keys[j];
-        const uint32_t d = (key >> shift) & 0xFFu;
-        const uint32_t out = s_base[d] + (j - s_start[d]);
+    for (uint32_t jj = t; jj < tile_n; jj += kSortThreads) {
+        const uint32_t key = s_keys[jj];
+        const uint32_t d = (key >> shift) & D::MASK;
+        const uint32_t out = s_base[d] + (jj - s_start[d]);
         keys_out[out] = key;
-        vals_out[out] = s_vals[j];
+        vals_out[out] = s_vals[jj];
     }
 }
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+template <int RB>
+int set_sort_attributes()
+{
+    TECTO_CUDA(cudaFuncSetAttribute(k_sort_pass<true, RB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)pass_smem<RB>(true)));
+    TECTO_CUDA(cudaFuncSetAttribute(k_sort_pass<false, RB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)pass_smem<RB>(false)));
+    return TECTO_OK;
+}
+
+bool g_sort_attr_done = false;
+
+template <int RB>
+int run_sort_rb(const SortArgs &a, const SortScratch &scr, cudaStream_t st, int *result_half)
+{
+    const int passes = scr.passes;
+    const size_t tiles = (a.n + kSortTile - 1) / kSortTile;
+    constexpr int R = Digits<RB>::R;
+    // one memset covers hist, status and counters (contiguous in the scratch layout)
+    const size_t clear = align256((size_t)passes * R * 4) + align256((size_t)passes * tiles * R * 4) +
+                         align256(kMaxSortPasses * 4);
+    TECTO_CUDA(cudaMemsetAsync(scr.hist, 0, clear, st));
+    const bool gen = a.worlds != nullptr;
+    const GenArgs g{a.worlds, a.vbase, a.nworlds, a.cur_id};
+    int hist_blocks = (int)((a.n + 255) / 256);
+    if (hist_blocks > 152 * 8) hist_blocks = 152 * 8;
+    if (gen)
+        k_sort_hist<true, RB><<<hist_blocks, 256, 0, st>>>(g, nullptr, a.n, passes, scr.hist);
+    else
+        k_sort_hist<false, RB><<<hist_blocks, 256, 0, st>>>(g, a.keys_in, a.n, passes, scr.hist);
+    k_sort_scan<RB><<<1, kSortThreads, 0, st>>>(scr.hist, passes);
+    int half = 0;
+    const uint32_t *kin = a.keys_in, *vin = a.vals_in;
+    for (int p = 0; p < passes; ++p) {
+        uint32_t *kout = a.keys[half], *vout = a.vals[half];
+        uint32_t *status = scr.status + (size_t)p * tiles * R;
+        if (p == 0 && gen)
+            k_sort_pass<true, RB><<<(unsigned)tiles, kSortThreads, pass_smem<RB>(true), st>>>(
+                g, nullptr, nullptr, kout, vout, a.n, 0, scr.hist, status, scr.counters + p, scr.error);
+        else
+            k_sort_pass<false, RB><<<(unsigned)tiles, kSortThreads, pass_smem<RB>(false), st>>>(
+                g, kin, vin, kout, vout, a.n, RB * p, scr.hist + (size_t)p * R, status, scr.counters + p,
+                scr.error);
+        kin = kout;
+        vin = vout;
+        half ^= 1;
+    }
+    TECTO_CUDA(cudaGetLastError());
+    *result_half = half ^ 1;
+    return TECTO_OK;
+}
+
 }  // namespace
+
+int sort_kernel_attributes()
+{
+    if (g_sort_attr_done) return TECTO_OK;
+    int rc;
+    if ((rc = set_sort_attributes<8>()) != TECTO_OK || (rc = set_sort_attributes<9>()) != TECTO_OK ||
+        (rc = set_sort_attributes<10>()) != TECTO_OK || (rc = set_sort_attributes<11>()) != TECTO_OK)
+        return rc;
+    g_sort_attr_done = true;
+    return TECTO_OK;
+}
 
 int key_bits_for(size_t n)
 {
@@ -256,27 +390,32 @@ int key_bits_for(size_t n)
     return b;
 }
 
-int sort_passes_for(int key_bits) { return (key_bits + 7) / 8; }
+bool valid_radix_bits(int rb) { return rb >= 8 && rb <= kMaxRadixBits; }
 
-size_t sort_scratch_bytes(size_t n, int key_bits)
+int sort_passes_for(int key_bits, int rb) { return (key_bits + rb - 1) / rb; }
+
+size_t sort_scratch_bytes(size_t n, int key_bits, int rb)
 {
-    const size_t passes = (size_t)sort_passes_for(key_bits);
+    const size_t passes = (size_t)sort_passes_for(key_bits, rb);
     const size_t tiles = (n + kSortTile - 1) / kSortTile;
-    return align256(passes * kRadix * 4) + align256(passes * tiles * kRadix * 4) +
-           align256(kMaxSortPasses * 4) + align256(4);
+    const size_t R = (size_t)1 << rb;
+    return align256(passes * R * 4) + align256(passes * tiles * R * 4) + align256(kMaxSortPasses * 4) +
+           align256(4);
 }
 
-void sort_scratch_carve(void *base, size_t n, int key_bits, SortScratch *out)
+void sort_scratch_carve(void *base, size_t n, int key_bits, int rb, SortScratch *out)
 {
-    const int passes = sort_passes_for(key_bits);
+    const int passes = sort_passes_for(key_bits, rb);
     const size_t tiles = (n + kSortTile - 1) / kSortTile;
+    const size_t R = (size_t)1 << rb;
     char *p = (char *)base;
     out->passes = passes;
     out->tiles = (int)tiles;
+    out->radix_bits = rb;
     out->hist = (uint32_t *)p;
-    p += align256((size_t)passes * kRadix * 4);
+    p += align256((size_t)passes * R * 4);
     out->status = (uint32_t *)p;
-    p += align256((size_t)passes * tiles * kRadix * 4);
+    p += align256((size_t)passes * tiles * R * 4);
     out->counters = (uint32_t *)p;
     p += align256(kMaxSortPasses * 4);
     out->error = (uint32_t *)p;
@@ -284,51 +423,26 @@ void sort_scratch_carve(void *base, size_t n, int key_bits, SortScratch *out)
 
 int run_sort(const SortArgs &a, const SortScratch &scr, cudaStream_t st, int *result_half)
 {
-    const int passes = sort_passes_for(a.key_bits);
-    if (passes != scr.passes || a.n == 0 || a.n > (size_t)kValueMask) {
+    const int rb = scr.radix_bits;
+    if (!valid_radix_bits(rb) || sort_passes_for(a.key_bits, rb) != scr.passes || a.n == 0 ||
+        a.n > (size_t)kValueMask || (a.n + kSortTile - 1) / kSortTile > (size_t)scr.tiles) {
         set_error("run_sort: scratch does not match the problem size");
         return TECTO_ERR_INVALID;
     }
-    const size_t tiles = (a.n + kSortTile - 1) / kSortTile;
-    // one memset covers hist, status and counters (contiguous in the scratch layout)
-    const size_t clear = align256((size_t)passes * kRadix * 4) +
-                         align256((size_t)passes * tiles * kRadix * 4) + align256(kMaxSortPasses * 4);
-    TECTO_CUDA(cudaMemsetAsync(scr.hist, 0, clear, st));
-    const bool gen = a.worlds != nullptr;
-    const GenArgs g{a.worlds, a.vbase, a.nworlds, a.cur_id};
-    if (gen && (a.nworlds < 1 || a.nworlds > kMaxBatchWorlds)) {
+    if (a.worlds != nullptr && (a.nworlds < 1 || a.nworlds > kMaxBatchWorlds)) {
         set_error("run_sort: batch world count out of range");
         return TECTO_ERR_INVALID;
     }
-    int hist_blocks = (int)((a.n + 255) / 256);
-    if (hist_blocks > 152 * 8) hist_blocks = 152 * 8;
-    if (gen)
-        k_sort_hist<true><<<hist_blocks, 256, 0, st>>>(g, nullptr, a.n,
-                                                        passes, scr.hist);
-    else
-        k_sort_hist<false><<<hist_blocks, 256, 0, st>>>(g, a.keys_in, a.n,
-                                                         passes, scr.hist);
-    k_sort_scan<<<1, kRadix, 0, st>>>(scr.hist, passes);
-    int half = 0;
-    const uint32_t *kin = a.keys_in, *vin = a.vals_in;
-    for (int p = 0; p < passes; ++p) {
-        uint32_t *kout = a.keys[half], *vout = a.vals[half];
-        uint32_t *status = scr.status + (size_t)p * tiles * kRadix;
-        if (p == 0 && gen)
-            k_sort_pass<true><<<(unsigned)tiles, kSortThreads, 0, st>>>(
-                g, nullptr, nullptr, kout, vout, a.n, 0, scr.hist,
-                status, scr.counters + p, scr.error);
-        else
-            k_sort_pass<false><<<(unsigned)tiles, kSortThreads, 0, st>>>(
-                g, kin, vin, kout, vout, a.n, 8 * p,
-                scr.hist + p * kRadix, status, scr.counters + p, scr.error);
-        kin = kout;
-        vin = vout;
-        half ^= 1;
+    if (rb > 8 && !g_sort_attr_done) {  // wide digits need the opt-in shared memory size
+        set_error("run_sort: sort kernel attributes not set");
+        return TECTO_ERR_INVALID;
     }
-    TECTO_CUDA(cudaGetLastError());
-    *result_half = half ^ 1;
-    return TECTO_OK;
+    switch (rb) {
+        case 8: return run_sort_rb<8>(a, scr, st, result_half);
+        case 9: return run_sort_rb<9>(a, scr, st, result_half);
+        case 10: return run_sort_rb<10>(a, scr, st, result_half);
+        default: return run_sort_rb<11>(a, scr, st, result_half);
+    }
 }
 
 }  // namespace tecto
@@ -339,7 +453,7 @@ extern "C" size_t tecto_sort_scratch_bytes(size_t n, int key_bits)
 {
     if (key_bits < 1 || key_bits > 32) return 0;
     // two ping-pong halves for keys and values are carved after the sort's own scratch
-    return tecto::sort_scratch_bytes(n, key_bits) + 4 * tecto::align256(n * sizeof(uint32_t));
+    return tecto::sort_scratch_bytes(n, key_bits, 8) + 4 * tecto::align256(n * sizeof(uint32_t));
 }
 
 extern "C" int tecto_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_out,
@@ -359,8 +473,8 @@ extern "C" int tecto_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in
     }
     cudaStream_t st = (cudaStream_t)stream;
     SortScratch scr{};
-    sort_scratch_carve(scratch, n, key_bits, &scr);
-    char *p = (char *)scratch + sort_scratch_bytes(n, key_bits);
+    sort_scratch_carve(scratch, n, key_bits, 8, &scr);
+    char *p = (char *)scratch + sort_scratch_bytes(n, key_bits, 8);
     const size_t arr = align256(n * sizeof(uint32_t));
     SortArgs a{};
     a.keys_in = keys_in;

@@ -14,7 +14,7 @@ namespace {
 
 constexpr size_t kMaxPairs = TECTO_SORT_NOALLOC_MAX_PAIRS;
 constexpr size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
-// sort_scratch_bytes(kMaxPairs, 32): histograms, look-back status (4 passes), counters, error word
+// sort_scratch_bytes(kMaxPairs, 32, 8): histograms, look-back status (4 passes), counters, error word
 constexpr size_t kSortPart = a256((size_t)kMaxSortPasses * 256 * 4) +
                              a256((size_t)kMaxSortPasses * ((kMaxPairs + kSortTile - 1) / kSortTile) * 256 * 4) +
                              a256((size_t)kMaxSortPasses * 4) + a256(4);
@@ -82,9 +82,9 @@ extern "C" int tecto_sort_pairs_noalloc(const uint32_t *keys_in, const uint32_t 
     if (rc != TECTO_OK) return rc;
     cudaStream_t st = (cudaStream_t)stream;
     SortScratch scr{};
-    sort_scratch_carve(base, n, key_bits, &scr);  // fits: sized for the maximum n and 4 passes
+    sort_scratch_carve(base, n, key_bits, 8, &scr);  // fits: sized for the maximum n and 4 passes
     char *half = (char *)base + kSortPart;
-    const int passes = sort_passes_for(key_bits);
+    const int passes = sort_passes_for(key_bits, 8);
     const int last = (passes - 1) & 1;  // the half the final pass writes: the caller's outputs
     SortArgs a{};
     a.keys_in = keys_in;

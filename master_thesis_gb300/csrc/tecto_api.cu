@@ -2,6 +2,7 @@
 // generator, field I/O, phase entry points and the step driver.  Replaces PlateTectonicSim
 // (src/cuda_compute/plate_tectonic_sim.h:110-130, plate_tectonic_sim.cu:28-131) for the
 // hot-path phases.  A world stepped on its own runs as a private batch of one (tecto_batch.cu).
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -137,7 +138,11 @@ size_t world_footprint(int W, int H)
     L.add(N * 4); L.add(N * 4); L.add(N * 4); L.add(N * 8); L.add(N * 4); L.add(N * 8); L.add(N * 4); L.add(N);
     L.add(kPairs); L.add(kDivWords * 4); L.add(kDivWords * 4); L.add(kPairs * sizeof(PairCounts));
     L.add(kPlates * sizeof(tecto_plate)); L.add((kPlates + 1) * sizeof(int2)); L.add(sizeof(Control));
-    return L.total + 4 * N * 4 + sort_scratch_bytes(N, 32) / 2;
+    // its share of a batch's sort: key/value ping-pong plus the scratch of the widest digit choice
+    size_t scratch = 0;
+    for (int rb = 8; rb <= kMaxRadixBits; ++rb)
+        scratch = std::max(scratch, sort_scratch_bytes(N, key_bits_for(N), rb));
+    return L.total + 4 * N * 4 + scratch;
 }
 
 }  // namespace tecto
@@ -592,6 +597,16 @@ int tecto_world_get_iteration(const tecto_world *w, uint32_t *iteration)
     from_batch(w, *b);                 \
     w->launches += b->launches - before; \
     return rc;
+
+int tecto_world_autotune(tecto_world *w, tecto_stream_t stream, tecto_tuning *out)
+{
+    int rc = check_world(w);
+    if (rc != TECTO_OK) return rc;
+    if ((rc = bind_device(w)) != TECTO_OK) return rc;
+    Batch *b = nullptr;
+    if ((rc = own_batch(w, &b)) != TECTO_OK) return rc;
+    return tune_batch(*b, (cudaStream_t)stream, out);
+}
 
 int tecto_phase_collide(tecto_world *w, tecto_stream_t stream)
 {

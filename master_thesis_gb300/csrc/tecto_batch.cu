@@ -2,6 +2,7 @@
 // batch-level buffers, ping-pong alignment of members, and the step driver with CUDA-graph
 // replay.  A world stepped on its own uses a private batch of one.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 
 #include "tecto_internal.cuh"
@@ -110,20 +111,42 @@ void batch_release(Batch &b)
     b.table_arena = nullptr;
     b.arena = nullptr;
     b.capacity = 0;
+    b.arena_bytes = 0;
     b.table_bytes = 0;
     b.members.clear();
 }
 
+// Tile variant and digit width: explicit settings first, then the autotuner's choice for this
+// batch (or its cached choice for the shape class), then the defaults.
+static void choose_tuning(const Batch &b, int *variant, int *rb)
+{
+    *variant = hydro_variant_for(b.settings);
+    if (*variant == 0) *variant = b.tuned_hydro ? b.tuned_hydro : kDefaultHydroVariant;
+    *rb = b.settings.step.sortRadixBits;
+    if (!valid_radix_bits(*rb)) *rb = valid_radix_bits(b.tuned_rb) ? b.tuned_rb : kDefaultRadixBits;
+}
+
 int batch_prepare(Batch &b, cudaStream_t st)
 {
-    const int variant = hydro_variant_for(b.settings);
-    if (!b.dirty && variant == b.hydro_variant) return TECTO_OK;
+    if (b.dirty && !b.members.empty()) {  // membership changed: cached autotuner choice, if any
+        size_t cells = 0;
+        for (const tecto_world *w : b.members) cells += w->N;
+        int th = 0, tr = 0;
+        if (tune_lookup(b.device, cells, b.members.size(), &th, &tr)) {
+            b.tuned_hydro = th;
+            b.tuned_rb = tr;
+        }
+    }
+    int variant = 0, rb = 0;
+    choose_tuning(b, &variant, &rb);
+    if (!b.dirty && variant == b.hydro_variant && rb == b.sort.radix_bits) return TECTO_OK;
     if (b.members.empty()) {
         set_error("batch has no worlds");
         return TECTO_ERR_INVALID;
     }
     int rc = ensure_kernel_attributes();
     if (rc != TECTO_OK) return rc;
+    if ((rc = sort_kernel_attributes()) != TECTO_OK) return rc;
     drop_graphs(b);
     b.hydro_variant = variant;
     const size_t n = b.members.size();
@@ -172,28 +195,33 @@ int batch_prepare(Batch &b, cudaStream_t st)
     for (int k = 0; k < TK_COUNT; ++k)
         TECTO_CUDA(cudaMemcpyAsync(b.d_tiles[k], tiles[k].data(), tiles[k].size() * sizeof(uint2),
                                    cudaMemcpyHostToDevice, st));
-    // batch-level buffers
-    if (total > b.capacity) {
-        if (b.arena) cudaFree(b.arena);
-        b.arena = nullptr;
-        b.capacity = 0;
-        const size_t cap = total;
-        const int kb = key_bits_for(cap);
-        const size_t arr = a256(cap * 4);
-        const size_t bytes = 4 * arr + a256(sizeof(BatchCtl)) + a256(sort_scratch_bytes(cap, kb));
-        TECTO_CUDA(cudaMalloc(&b.arena, bytes));
-        TECTO_CUDA(cudaMemsetAsync(b.arena, 0, bytes, st));
-        char *q = (char *)b.arena;
-        b.keys[0] = (uint32_t *)q;
-        b.keys[1] = (uint32_t *)(q + arr);
-        b.vals[0] = (uint32_t *)(q + 2 * arr);
-        b.vals[1] = (uint32_t *)(q + 3 * arr);
-        b.bctl = (BatchCtl *)(q + 4 * arr);
-        b.capacity = cap;
+    // batch-level buffers: key/value ping-pong for `capacity` cells, the control block, then the
+    // sort scratch of the current size and digit width
+    const int kb = key_bits_for(total);
+    {
+        const size_t cap = std::max(b.capacity, total);
+        const size_t need = 4 * a256(cap * 4) + a256(sizeof(BatchCtl)) + a256(sort_scratch_bytes(total, kb, rb));
+        if (need > b.arena_bytes) {
+            if (b.arena) cudaFree(b.arena);
+            b.arena = nullptr;
+            b.capacity = 0;
+            b.arena_bytes = 0;
+            TECTO_CUDA(cudaMalloc(&b.arena, need));
+            TECTO_CUDA(cudaMemsetAsync(b.arena, 0, need, st));
+            const size_t arr = a256(cap * 4);
+            char *q = (char *)b.arena;
+            b.keys[0] = (uint32_t *)q;
+            b.keys[1] = (uint32_t *)(q + arr);
+            b.vals[0] = (uint32_t *)(q + 2 * arr);
+            b.vals[1] = (uint32_t *)(q + 3 * arr);
+            b.bctl = (BatchCtl *)(q + 4 * arr);
+            b.capacity = cap;
+            b.arena_bytes = need;
+        }
     }
     {
         char *q = (char *)b.arena + 4 * a256(b.capacity * 4) + a256(sizeof(BatchCtl));
-        sort_scratch_carve(q, total, key_bits_for(total), &b.sort);
+        sort_scratch_carve(q, total, kb, rb, &b.sort);
     }
     // the error word may now sit where a larger batch kept look-back status words
     TECTO_CUDA(cudaMemsetAsync(b.sort.error, 0, 4, st));
@@ -334,6 +362,36 @@ int tecto_batch_step(tecto_batch *batch, int nSteps, tecto_stream_t stream)
     if (!batch || nSteps < 0) return TECTO_ERR_INVALID;
     if (batch->b.members.empty()) return TECTO_OK;
     return batch_step(batch->b, nSteps, (cudaStream_t)stream);
+}
+
+int tecto_batch_phase_hydraulic(tecto_batch *batch, int iterations, float dt, tecto_stream_t stream)
+{
+    if (!batch || iterations < 0 || !std::isfinite(dt)) return TECTO_ERR_INVALID;
+    Batch &b = batch->b;
+    if (b.members.empty()) return TECTO_OK;
+    const cudaStream_t st = (cudaStream_t)stream;
+    int rc = batch_prepare(b, st);
+    if (rc != TECTO_OK) return rc;
+    const uint64_t before = b.launches;
+    rc = launch_hydraulic(b, iterations, dt, st);
+    for (tecto_world *w : b.members) w->launches += b.launches - before;
+    sync_members(b);
+    return rc;
+}
+
+int tecto_batch_phase_thermal(tecto_batch *batch, int iterations, tecto_stream_t stream)
+{
+    if (!batch || iterations < 0) return TECTO_ERR_INVALID;
+    Batch &b = batch->b;
+    if (b.members.empty()) return TECTO_OK;
+    const cudaStream_t st = (cudaStream_t)stream;
+    int rc = batch_prepare(b, st);
+    if (rc != TECTO_OK) return rc;
+    const uint64_t before = b.launches;
+    rc = launch_thermal(b, iterations, st);
+    for (tecto_world *w : b.members) w->launches += b.launches - before;
+    sync_members(b);
+    return rc;
 }
 
 int tecto_batch_size(const tecto_batch *batch, int *worlds, size_t *cells)

@@ -24,6 +24,7 @@ constexpr int kSortTile = 4096;                 // keys per onesweep tile (256 t
 constexpr int kSortThreads = 256;
 constexpr int kSortItems = kSortTile / kSortThreads;
 constexpr int kMaxSortPasses = 4;               // 32-bit keys, 8-bit digits
+constexpr int kMaxRadixBits = 11;              // widest sort digit
 constexpr int kMaxBatchWorlds = 1024;           // worlds per batch (world lookup table in smem)
 
 // Status word of the decoupled look-back: 2 flag bits + 30 value bits.
@@ -60,12 +61,13 @@ struct BatchCtl {
 
 // Scratch of the radix sort (histograms, look-back status).  Sizes in tecto_sort_scratch_bytes.
 struct SortScratch {
-    uint32_t *hist;      // [passes][256] digit counts -> exclusive digit starts
-    uint32_t *status;    // [passes][tiles][256] look-back words
+    uint32_t *hist;      // [passes][2^radix_bits] digit counts -> exclusive digit starts
+    uint32_t *status;    // [passes][tiles][2^radix_bits] look-back words
     uint32_t *counters;  // [passes] dynamic tile counters
     uint32_t *error;     // error flag word
     int passes;
     int tiles;
+    int radix_bits;      // digit width, 8..kMaxRadixBits
 };
 
 // Device descriptor of one world (one cudaMalloc'd arena per world, structure of arrays).
@@ -108,6 +110,8 @@ struct Batch {
     int sort_final = 0;
     size_t total = 0;                        // sum of member cells
     int hydro_variant = 0;                   // tile variant the TK_HYDRO list was built for
+    int tuned_hydro = 0, tuned_rb = 0;       // autotuner's choices (0 = none), used when the
+                                             // settings leave hydraulicTile / sortRadixBits at 0
     uint64_t launches = 0;
     bool dirty = true;                       // tables must be rebuilt before the next launch
     // device tables
@@ -122,6 +126,7 @@ struct Batch {
     void *arena = nullptr;
     uint32_t *keys[2] = {};
     uint32_t *vals[2] = {};
+    size_t arena_bytes = 0;
     BatchCtl *bctl = nullptr;
     SortScratch sort{};
     // graphs of one step keyed by (cur_h, cur_wsf, cur_id, ccl)
@@ -240,7 +245,15 @@ int launch_bump_iteration(Batch &b, cudaStream_t st);
 int launch_ccl(Batch &b, int connectivity, bool due_only, cudaStream_t st);
 void gaussian_weights(float sigma, int radius, float *out);
 int ensure_kernel_attributes();
-int hydro_variant_for(const tecto_settings &s);
+int hydro_variant_for(const tecto_settings &s);  // 0 when the settings leave the choice open
+constexpr int kDefaultRadixBits = 8;
+constexpr int kHydroVariantCount = 5;
+constexpr int kDefaultHydroVariant = 4;          // 64 x 32 cells, 1024 threads
+
+// Autotuner cache (tecto_tune.cu): best hydraulic tile variant and sort digit width for a batch
+// shape class on a device; false when nothing was tuned for that class.
+bool tune_lookup(int device, size_t total_cells, size_t worlds, int *hydro, int *rb);
+int tune_batch(Batch &b, cudaStream_t st, tecto_tuning *out);  // tune on the members' shapes, apply
 
 // Radix sort core (k_sort.cu).  If worlds != nullptr the first pass generates the keys (the
 // batch-virtual destination cell of every virtual cell) and values (the virtual source cell)
@@ -258,10 +271,12 @@ struct SortArgs {
     size_t n;
     int key_bits;
 };
-int sort_passes_for(int key_bits);
-size_t sort_scratch_bytes(size_t n, int key_bits);
-void sort_scratch_carve(void *base, size_t n, int key_bits, SortScratch *out);
+bool valid_radix_bits(int rb);
+int sort_passes_for(int key_bits, int rb);
+size_t sort_scratch_bytes(size_t n, int key_bits, int rb);
+void sort_scratch_carve(void *base, size_t n, int key_bits, int rb, SortScratch *out);
 int run_sort(const SortArgs &a, const SortScratch &scr, cudaStream_t st, int *result_half);
+int sort_kernel_attributes();  // once, outside graph capture, before any digit width above 8
 
 int key_bits_for(size_t n);
 
