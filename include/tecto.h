@@ -401,6 +401,11 @@ int tecto_world_launch_count(const tecto_world *world, uint64_t *count);
 /* Wait for the world's stream work and report device-side error flags (bounded waits that gave
  * up) as TECTO_ERR_DEVICE_TIMEOUT. */
 int tecto_world_check(tecto_world *world, tecto_stream_t stream);
+/* Self-test of the division the erosion kernels use where a divisor repeats (Markstein's
+ * correction of a reciprocal product, with an IEEE-division fallback outside its safe range):
+ * out[i] = a[i] / b[i] computed that way, on device buffers.  Tests compare it bit for bit with
+ * the IEEE quotient. */
+int tecto_selftest_div(const float *a, const float *b, float *out, size_t n, tecto_stream_t stream);
 const char *tecto_last_error_string(void);
 const char *tecto_version(void);
 

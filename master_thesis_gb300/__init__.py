@@ -256,6 +256,7 @@ def _declare(L: C.CDLL) -> None:
         "tecto_server_run_trace_sequential": ([P, C.POINTER(Request), C.c_int, P, C.POINTER(RequestResult),
                                                C.POINTER(ServerStats)], C.c_int),
         "tecto_server_set_dry_cost": ([P, C.c_double], C.c_int),
+        "tecto_selftest_div": ([P, P, P, C.c_size_t, P], C.c_int),
         "tecto_last_error_string": ([], C.c_char_p),
         "tecto_version": ([], C.c_char_p),
     }
