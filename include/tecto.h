@@ -111,6 +111,9 @@ typedef struct tecto_simulation_settings {
 /* Uplift modes. */
 #define TECTO_UPLIFT_GAUSSIAN 0  /* +upliftAmount on convergent cells, separable Gaussian blur */
 #define TECTO_UPLIFT_NONE 1      /* no uplift phase */
+#define TECTO_UPLIFT_REFERENCE 2 /* the reference's uplift: continental collisions propagated against the
+                                    plate motion, a jump-flooding distance field to the nearest
+                                    collision, distance profiles applied (plate_tectonic_sim.cu:270-317) */
 
 /* CCL connectivity modes. */
 #define TECTO_CCL_4 4

@@ -31,7 +31,7 @@ MAX_PLATES = 255
 NUM_PAIRS = 32385
 NUM_DIV_WORDS = 1013
 
-UPLIFT_GAUSSIAN, UPLIFT_NONE = 0, 1
+UPLIFT_GAUSSIAN, UPLIFT_NONE, UPLIFT_REFERENCE = 0, 1, 2
 CCL_4, CCL_8, CCL_REF8 = 4, 8, 9
 
 (FIELD_HEIGHT, FIELD_WATER, FIELD_SEDIMENT, FIELD_FLUX, FIELD_PLATE_ID, FIELD_LABELS,

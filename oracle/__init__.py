@@ -41,6 +41,13 @@ def lib() -> C.CDLL:
         L.or_collision_words.argtypes = [C.c_int, C.c_int, V, V, V, V, V, V, V]
         L.or_collision_types.argtypes = [C.c_int, C.c_int, V, V, V, V, V, V]
         L.or_resolve.argtypes = [C.c_int, C.c_int, V, V, V, V, V, V, V, V, C.c_uint32, C.c_uint32, V, V, V]
+        L.or_resolve_ex.argtypes = [C.c_int, C.c_int, V, V, V, V, V, V, V, V, C.c_uint32, C.c_uint32, V, V, V,
+                                    V, V]
+        L.or_uplift_ref.argtypes = [C.c_int, C.c_int, V, V, V, V, V, V, V, V, V, V]
+        L.or_expf.argtypes = [C.c_float]
+        L.or_expf.restype = C.c_float
+        L.or_log10f.argtypes = [C.c_float]
+        L.or_log10f.restype = C.c_float
         L.or_thermal.argtypes = [C.c_int, C.c_int, V, C.c_int, V]
         L.or_hydraulic.argtypes = [C.c_int, C.c_int, V, V, V, V, C.c_int, C.c_float, C.c_uint32, V]
         L.or_accretion.argtypes = [C.c_int, C.c_int, V, V, V, V]
@@ -82,6 +89,7 @@ def ref() -> C.CDLL:
         L.ref_register_collisions.argtypes = [C.c_int, C.c_int, V, V, V]
         L.ref_collision_types.argtypes = [C.c_int, C.c_int, V, V, V, V, V]
         L.ref_process_collisions.argtypes = [C.c_int, C.c_int, V, V, V, V, V, V, C.c_int, C.c_uint, V, V, V, V, V]
+        L.ref_uplift.argtypes = [C.c_int, C.c_int, V, V, V, V, V, V, V, V, V]
         L.ref_thermal.argtypes = [C.c_int, C.c_int, V]
         L.ref_hydraulic.argtypes = [C.c_int, C.c_int, V, V, V, V, C.c_int, C.c_float, C.c_uint]
         L.ref_hydraulic.restype = C.c_int
@@ -128,6 +136,39 @@ def resolve(id_old, h_old, word, offx, offy, bitmap, div_bitmap, settings, seed,
     lib().or_resolve(W, H, _P(id_old), _P(h_old), _P(word), _P(offx), _P(offy), _P(bitmap), _P(div),
                      C.addressof(settings), seed, iteration, _P(h_new), _P(id_new), _P(acc))
     return h_new, id_new, acc, div
+
+
+def resolve_ex(id_old, h_old, word, offx, offy, bitmap, div_bitmap, settings, seed, iteration):
+    """resolve() plus the processConvergence records (heightAddition, typeByte) of convergent cells."""
+    H, W = id_old.shape
+    div = div_bitmap.copy()
+    h_new = np.zeros_like(h_old)
+    id_new = np.zeros_like(id_old)
+    acc = np.zeros_like(id_old)
+    up_h = np.zeros((H, W), np.float32)
+    up_t = np.zeros((H, W), np.uint8)
+    lib().or_resolve_ex(W, H, _P(id_old), _P(h_old), _P(word), _P(offx), _P(offy), _P(bitmap), _P(div),
+                        C.addressof(settings), seed, iteration, _P(h_new), _P(id_new), _P(acc), _P(up_h), _P(up_t))
+    return h_new, id_new, acc, div, up_h, up_t
+
+
+def uplift_ref(word, up_h, up_t, h_old, plates, id_new, h_new, settings):
+    """The reference uplift on resolved heights: (heights, JFA nearest seed, JFA distance)."""
+    H, W = h_old.shape
+    out = h_new.copy()
+    seed = np.zeros((H, W), np.int32)
+    dist = np.zeros((H, W), np.int32)
+    lib().or_uplift_ref(W, H, _P(word), _P(up_h), _P(up_t), _P(h_old), _P(plates), _P(id_new), _P(out),
+                        C.addressof(settings.kernel), _P(seed), _P(dist))
+    return out, seed, dist
+
+
+def expf(x: float) -> float:
+    return lib().or_expf(x)
+
+
+def log10f(x: float) -> float:
+    return lib().or_log10f(x)
 
 
 def thermal(h, iters, settings):

@@ -10,6 +10,7 @@
  */
 #include <cstdint>
 #include <cstring>
+#include <utility>
 #include <vector>
 
 #include "plate_tectonics_kernel.cuh"
@@ -150,6 +151,59 @@ void ref_process_collisions(int W, int H, const uint8_t *id_old, const float *h_
     for (size_t i = 0; i < N; ++i) {
         if (uplift_height) uplift_height[i] = up[i].cumulativeHeight;
         if (uplift_types) uplift_types[i] = up[i].collisionTypes;
+    }
+}
+
+/* The reference uplift (plate_tectonic_sim.cu:270-317): moveContinentalCollisions,
+ * combinePropagatedCollisions, JFAInitialize, JFAPass from the largest power of two below
+ * max(W, H) down to 1, JFAComputeDistance, applyUplift.  word / up_h / up_t: this step's arrival
+ * words and processConvergence records; h_old: heights before the step; plates: plate records
+ * before their centre update; h_new updated in place.  The plate table gets a 256th, all-zero
+ * record: applyUplift can name plate 255 when merged type bits point at an empty slot, which reads
+ * past the reference's 255-entry table. */
+void ref_uplift(int W, int H, const uint32_t *word, const float *up_h, const uint8_t *up_t,
+                const float *h_old, const tecto_plate *plates, const uint8_t *id_new, float *h_new,
+                int32_t *jfa_seed, int32_t *jfa_dist)
+{
+    const size_t N = (size_t)W * H;
+    std::vector<UpliftData> up(N);
+    for (size_t i = 0; i < N; ++i) up[i] = UpliftData(up_h[i], up_t[i]);
+    std::vector<uint32_t> wc(word, word + N);
+    std::vector<float> hc(h_old, h_old + N);
+    std::vector<uint8_t> idc(id_new, id_new + N);
+    std::vector<PropagatedUpliftData> prop(N);
+    std::vector<PlateData> pd = make_plates(plates);
+    pd.resize(MAX_PLATE_COUNT + 1);
+    pd[MAX_PLATE_COUNT].direction = Vec2<float>(0.0f, 0.0f);
+    pd[MAX_PLATE_COUNT].pixelCenter = Vec2<float>(0.0f, 0.0f);
+    pd[MAX_PLATE_COUNT].velocity = 0.0f;
+    CudaTexture<UpliftData> tUp(up.data(), Vec2<int>(W, H));
+    CudaTexture<uint32_t> tWord(wc.data(), Vec2<int>(W, H));
+    CudaTexture<float> tH(hc.data(), Vec2<int>(W, H)), tHNew(h_new, Vec2<int>(W, H));
+    CudaTexture<PropagatedUpliftData> tProp(prop.data(), Vec2<int>(W, H));
+    CudaTexture<uint8_t> tId(idc.data(), Vec2<int>(W, H));
+    launch(blocks_for(N), TPB, [&] { moveContinentalCollisions(&tUp, &tWord, &tH, &tProp, pd.data()); });
+    launch(blocks_for(N), TPB, [&] { combinePropagatedCollisions(&tUp, &tWord, &tProp); });
+    std::vector<int> ja(N), jb(N);
+    CudaTexture<int> tA(ja.data(), Vec2<int>(W, H)), tB(jb.data(), Vec2<int>(W, H));
+    launch(blocks_for(N), TPB, [&] { JFAInitialize(&tProp, &tA); });
+    const int maxDim = W > H ? W : H;
+    int step = 1;
+    while (step < maxDim) step <<= 1;
+    step >>= 1;
+    CudaTexture<int> *a = &tA, *b = &tB;
+    while (step > 0) {
+        launch(blocks_for(N), TPB, [&] { JFAPass(a, b, step); });
+        std::swap(a, b);
+        step >>= 1;
+    }
+    std::vector<DistanceFieldBuffer> dfb(N);
+    CudaTexture<DistanceFieldBuffer> tD(dfb.data(), Vec2<int>(W, H));
+    launch(blocks_for(N), TPB, [&] { JFAComputeDistance(a, &tD); });
+    launch(blocks_for(N), TPB, [&] { applyUplift(&tId, &tProp, &tD, pd.data(), &tHNew); });
+    for (size_t i = 0; i < N; ++i) {
+        if (jfa_seed) jfa_seed[i] = (*a)[Vec2<int>((int)(i % W), (int)(i / W))];
+        if (jfa_dist) jfa_dist[i] = dfb[i].dist;
     }
 }
 

@@ -154,6 +154,8 @@ float or_lerp(float a, float b, float t)
 static int g_libm_sin = 0;
 void or_use_libm_sin(int on) { g_libm_sin = on; }
 float or_sinf(float x) { return g_libm_sin ? sinf(x) : tecto_sinf(x); }
+float or_expf(float x) { return tecto_expf(x); }
+float or_log10f(float x) { return tecto_log10f(x); }
 
 /* ---- plate kinematics ------------------------------------------------------------------ */
 
@@ -344,6 +346,17 @@ void or_resolve(int W, int H, const uint8_t *id_old, const float *h_old, const u
                 const tecto_settings *st, uint32_t seed, uint32_t iteration, float *h_new,
                 uint8_t *id_new, uint8_t *acc)
 {
+    or_resolve_ex(W, H, id_old, h_old, word, off_x, off_y, bm, div_bitmap, st, seed, iteration, h_new,
+                  id_new, acc, NULL, NULL);
+}
+
+/* processCollisions plus the UpliftData record of every convergent cell (up_h = heightAddition,
+ * up_t = typeByte, processConvergence :501-582); up_h / up_t may be NULL. */
+void or_resolve_ex(int W, int H, const uint8_t *id_old, const float *h_old, const uint32_t *word,
+                   const int32_t *off_x, const int32_t *off_y, const uint8_t *bm, uint32_t *div_bitmap,
+                   const tecto_settings *st, uint32_t seed, uint32_t iteration, float *h_new,
+                   uint8_t *id_new, uint8_t *acc, float *up_h, uint8_t *up_t)
+{
     const tecto_kernel_settings *ks = &st->kernel;
     const size_t N = (size_t)W * (size_t)H;
     uint32_t has_div[TECTO_NUM_DIV_WORDS];
@@ -409,6 +422,8 @@ void or_resolve(int W, int H, const uint8_t *id_old, const float *h_old, const u
             if (!sub[i]) owner = i;
         const uint8_t ownerId = ids[owner];
         float writeH = heights[owner];
+        float hadd = 0.0f;
+        uint8_t tbyte = 0;
         for (int a = 0; a < pairLen; ++a) {
             const int ia = PL[a][0], ib = PL[a][1];
             float hh;
@@ -416,7 +431,12 @@ void or_resolve(int W, int H, const uint8_t *id_old, const float *h_old, const u
             else if (ib == owner) hh = heights[ia];
             else continue;
             if (hh > writeH) { const float tmp = hh; hh = writeH; writeH = tmp; }
+            hadd = hadd + hh;
             const uint32_t t = types[a];
+            if (ia == owner)
+                tbyte |= (uint8_t)(((t == 2 ? 0 : 1) & 1) | ((ia & 3) << 1) | ((ib & 3) << 3));
+            else
+                tbyte |= (uint8_t)(((t == 1 ? 0 : 1) & 1) | ((ib & 3) << 1) | ((ia & 3) << 3));
             int other = -1;
             if (ia == owner && t == 4) other = ib;
             else if (ib == owner && t == 3) other = ia;
@@ -432,6 +452,8 @@ void or_resolve(int W, int H, const uint8_t *id_old, const float *h_old, const u
         }
         h_new[d] = writeH;
         id_new[d] = ownerId;
+        if (up_h) up_h[d] = hadd;
+        if (up_t) up_t[d] = tbyte;
     }
     /* flipDivergedBitmap (:772-780) */
     for (int i = 0; i < TECTO_NUM_DIV_WORDS; ++i) div_bitmap[i] ^= has_div[i];
@@ -462,6 +484,249 @@ void or_resolve(int W, int H, const uint8_t *id_old, const float *h_old, const u
             }
         free(tmp);
     }
+}
+
+/* ---- reference uplift: continental propagation, JFA distance field, applyUplift ------------- */
+
+typedef struct {
+    int x, y;
+} iv2;
+
+/* continentalPropagation (plate_tectonics_kernel.cu:975-1027): march from p against the plate's
+ * motion (a DDA over cell edges) while the old height stays at or above continentalPropThreshold;
+ * the returned coordinate is not wrapped (heights are read through the torus). */
+static iv2 cont_prop(int W, int H, const float *h_old, iv2 p, const tecto_plate *pd, float start,
+                     const tecto_kernel_settings *ks)
+{
+    if (start < ks->continentalPropThreshold) return p;
+    const float posx = (float)p.x + pd->pixelCenter_x, posy = (float)p.y + pd->pixelCenter_y;
+    const int stepX = -pd->direction_x > 0 ? 1 : -1;
+    const int stepY = -pd->direction_y > 0 ? 1 : -1;
+    const float tdx = fabsf(1.0f / -pd->direction_x), tdy = fabsf(1.0f / -pd->direction_y);
+    const int nextX = stepX > 0 ? p.x + 1 : p.x, nextY = stepY > 0 ? p.y + 1 : p.y;
+    float tmx = ((float)nextX - posx) / -pd->direction_x;
+    float tmy = ((float)nextY - posy) / -pd->direction_y;
+    iv2 prev = p;
+    for (int i = 0; i < ks->continentalPropMaxIters; ++i) {
+        if (tmx < tmy) {
+            p.x += stepX;
+            tmx = tmx + tdx;
+        } else {
+            p.y += stepY;
+            tmy = tmy + tdy;
+        }
+        if (h_old[cidx(p.x, p.y, W, H)] < ks->continentalPropThreshold) return p;
+        prev = p;
+    }
+    return prev;
+}
+
+/* atomicInsertPlatePair (:1029-1071) executed alone: both plates (as 255 - id bytes) go into free
+ * bytes of the packed word, plates already present are skipped, nothing is written unless both fit. */
+static int insert_pair(uint32_t *inv, int a, int b)
+{
+    uint32_t ins[2] = {255u - (uint32_t)a, 255u - (uint32_t)b};
+    const uint32_t old = *inv;
+    uint32_t nw = old;
+    for (int i = 0; i < 4; ++i) {
+        const uint32_t pl = (old >> (8 * i)) & 0xFFu;
+        for (int j = 0; j < 2; ++j) {
+            if (pl == 0 && ins[j] != 0) {
+                nw |= ins[j] << (8 * i);
+                ins[j] = 0;
+                break;
+            }
+            if (pl == ins[j]) ins[j] = 0;
+        }
+    }
+    if (ins[0] != 0 || ins[1] != 0) return 0;
+    *inv = nw;
+    return 1;
+}
+
+/* countCollision (:1073-1085) */
+static void count_at(iv2 pos, iv2 *positions, int *counts, int *total, int inc)
+{
+    for (int i = 0; i < 6; ++i)
+        if (counts[i] == 0 || (positions[i].x == pos.x && positions[i].y == pos.y)) {
+            positions[i] = pos;
+            counts[i] += inc;
+            *total += inc;
+            return;
+        }
+}
+
+static float subduction_under(float x)
+{
+    const float v = tecto_log10f(1.0f + 8.0f * (x - 1.0f)) / 1.908485019f - 1.0f;
+    return fminf(v, 0.0f);
+}
+
+static float continental_profile(float x)
+{
+    return tecto_expf(-0.02f * x * x) + tecto_expf(-0.2f * x * x) * (0.5f - fabsf(fmodf(fabsf(x), 1.0f) - 0.5f));
+}
+
+static int jfa_dist2(int cx, int cy, int seed, int W, int H)
+{
+    const int sx = seed % W, sy = seed / W;
+    int dx = abs(cx - sx), dy = abs(cy - sy);
+    dx = dx < W - dx ? dx : W - dx;
+    dy = dy < H - dy ? dy : H - dy;
+    return dx * dx + dy * dy;
+}
+
+/* The reference uplift of one step (plate_tectonic_sim.cu:270-317), every kernel run as one
+ * sequential pass in ascending cell order - the canonical order of its atomic inserts and adds:
+ * moveContinentalCollisions (:1087-1185), combinePropagatedCollisions (:1187-1218),
+ * JFAInitialize / JFAPass / JFAComputeDistance (:1498-1600), applyUplift (:1662-1738).
+ * word: this step's arrival words; up_h / up_t: processConvergence's records (valid where the word
+ * holds two plates or more); h_old: heights before the step; plates: plate records before their
+ * centre update; id_new / h_new: resolved ids and heights, h_new updated in place.  jfa_seed /
+ * jfa_dist (optional outputs): the nearest propagated collision cell and its distance, -1 none. */
+void or_uplift_ref(int W, int H, const uint32_t *word, const float *up_h, const uint8_t *up_t,
+                   const float *h_old, const tecto_plate *plates, const uint8_t *id_new, float *h_new,
+                   const tecto_kernel_settings *ks, int32_t *jfa_seed, int32_t *jfa_dist)
+{
+    const size_t N = (size_t)W * (size_t)H;
+    float *ph = (float *)calloc(N, sizeof(float));
+    uint32_t *pinv = (uint32_t *)calloc(N, sizeof(uint32_t));
+    uint8_t *pt = (uint8_t *)calloc(N, 1);
+    int32_t *ja = (int32_t *)malloc(N * sizeof(int32_t));
+    int32_t *jb = (int32_t *)malloc(N * sizeof(int32_t));
+    /* moveContinentalCollisions */
+    for (size_t d = 0; d < N; ++d) {
+        const uint32_t cp = word[d];
+        if ((cp >> 8) == 0) continue;
+        if ((up_t[d] & 1) != 1) continue;
+        const int pidx = (up_t[d] >> 1) & 3;
+        const int primary = 255 - (int)((cp >> (8 * pidx)) & 0xFFu);
+        const iv2 pos = {(int)(d % (size_t)W), (int)(d / (size_t)W)};
+        const float cur = h_old[d];
+        const iv2 ppos = cont_prop(W, H, h_old, pos, &plates[primary], cur, ks);
+        iv2 positions[6];
+        int counts[6] = {0, 0, 0, 0, 0, 0}, total = 0;
+        for (int k = 0; k < 4; ++k) {
+            const int sec = 255 - (int)((cp >> (8 * k)) & 0xFFu);
+            if (sec == 255 || sec == primary) continue;
+            const iv2 spos = cont_prop(W, H, h_old, pos, &plates[sec], cur, ks);
+            if (ppos.x == spos.x && ppos.y == spos.y) {
+                if (insert_pair(&pinv[cidx(ppos.x, ppos.y, W, H)], primary, sec))
+                    count_at(ppos, positions, counts, &total, 2);
+            } else {
+                if (insert_pair(&pinv[cidx(ppos.x, ppos.y, W, H)], primary, sec))
+                    count_at(ppos, positions, counts, &total, 1);
+                if (insert_pair(&pinv[cidx(spos.x, spos.y, W, H)], primary, sec))
+                    count_at(spos, positions, counts, &total, 1);
+            }
+            count_at(ppos, positions, counts, &total, 1);
+            count_at(spos, positions, counts, &total, 1);
+        }
+        for (int i = 0; i < 6; ++i) {
+            if (counts[i] == 0) break;
+            const uint32_t t = cidx(positions[i].x, positions[i].y, W, H);
+            ph[t] = ph[t] + (up_h[d] / (float)total) * (float)counts[i];
+        }
+    }
+    /* combinePropagatedCollisions (cells without two plates never become JFA seeds, so their
+     * non-seed record is taken as is) */
+    for (size_t d = 0; d < N; ++d) {
+        if (pinv[d] != 0) {
+            pt[d] = 1;
+        } else if ((word[d] >> 8) != 0) {
+            if ((up_t[d] & 1) == 0) {
+                pt[d] = up_t[d];
+                ph[d] = up_h[d];
+                pinv[d] = word[d];
+            } else {
+                pinv[d] = 1;
+            }
+        } else {
+            pinv[d] = word[d];
+        }
+    }
+    /* JFAInitialize */
+    for (size_t d = 0; d < N; ++d) ja[d] = (pinv[d] >> 8) != 0 ? (int32_t)d : -1;
+    /* JFAPass, steps from the largest power of two below max(W, H) down to 1 */
+    const int maxDim = W > H ? W : H;
+    int step = 1;
+    while (step < maxDim) step <<= 1;
+    step >>= 1;
+    while (step > 0) {
+#pragma omp parallel for schedule(static)
+        for (int y = 0; y < H; ++y)
+            for (int x = 0; x < W; ++x) {
+                const size_t d = (size_t)y * W + x;
+                int best = ja[d], bestDist = 0x7FFFFFFF;
+                if (best >= 0) bestDist = jfa_dist2(x, y, best, W, H);
+                for (int oy = -1; oy <= 1; ++oy)
+                    for (int ox = -1; ox <= 1; ++ox) {
+                        if (ox == 0 && oy == 0) continue;
+                        const int cand = ja[cidx(x + ox * step, y + oy * step, W, H)];
+                        if (cand < 0) continue;
+                        const int dist = jfa_dist2(x, y, cand, W, H);
+                        if (dist < bestDist) {
+                            bestDist = dist;
+                            best = cand;
+                        }
+                    }
+                jb[d] = best;
+            }
+        int32_t *tmp = ja;
+        ja = jb;
+        jb = tmp;
+        step >>= 1;
+    }
+    /* JFAComputeDistance + applyUplift */
+    for (size_t d = 0; d < N; ++d) {
+        const int x = (int)(d % (size_t)W), y = (int)(d / (size_t)W);
+        const int seed = ja[d];
+        int dist = -1;
+        uint32_t orig = 0;
+        if (seed >= 0) {
+            dist = (int)sqrtf((float)jfa_dist2(x, y, seed, W, H));
+            orig = (uint32_t)seed;
+        }
+        if (jfa_seed) jfa_seed[d] = seed;
+        if (jfa_dist) jfa_dist[d] = dist;
+        if (dist <= -1) continue;
+        const uint8_t ct = pt[orig];
+        const uint32_t inv = pinv[orig];
+        const int type = ct & 1, pi = (ct >> 1) & 3, si = (ct >> 3) & 3;
+        const int prim = 255 - (int)((inv >> (8 * pi)) & 0xFFu);
+        const int secp = 255 - (int)((inv >> (8 * si)) & 0xFFu);
+        const int plate = id_new[d];
+        if (type == 0 && secp == plate) {
+            const float value = subduction_under((float)dist);
+            const float mult = 1.0f + value * ks->subductionUnderUpliftMultiplier;
+            h_new[d] = fmaxf(h_new[d] * mult, ks->minUpliftClamp);
+        } else if (type == 0 && prim == plate) {
+            const int ox = (int)(orig % (uint32_t)W), oy = (int)(orig / (uint32_t)W);
+            const float sx = (float)W, sy = (float)H;
+            const float ddx = fmodf((float)(x - ox) + sx * 0.5f, sx) - sx * 0.5f;
+            const float ddy = fmodf((float)(y - oy) + sy * 0.5f, sy) - sy * 0.5f;
+            float mag = sqrtf(ddx * ddx + ddy * ddy);
+            mag = fmaxf(mag, 1e-20f);
+            const float dirx = ddx / mag, diry = ddy / mag;
+            /* plate 255 (an empty slot named by merged type bits) has no record: zero direction */
+            const float odx = secp < 255 ? plates[secp].direction_x : 0.0f;
+            const float ody = secp < 255 ? plates[secp].direction_y : 0.0f;
+            const float dot = fmaxf(dirx * odx + diry * ody, 0.0f);
+            const float value = continental_profile(((float)dist - (float)ks->subductionOverRange) - 10.0f);
+            const float mult = 1.0f + (value * dot) * ks->subductionOverUpliftMultiplier;
+            h_new[d] = fmaxf(h_new[d] * mult, ks->minUpliftClamp);
+        } else if (type == 1) {
+            const float height = ph[orig];
+            const float value = continental_profile((float)dist);
+            const float change = (value * height) * ks->continentalUpliftMultiplier;
+            h_new[d] = fminf(h_new[d] + change, ks->maxUpliftClamp);
+        }
+    }
+    free(ph);
+    free(pinv);
+    free(pt);
+    free(ja);
+    free(jb);
 }
 
 /* ---- thermal ------------------------------------------------------------------------------- */
@@ -733,7 +998,16 @@ void or_step(int W, int H, float *h, float *w, float *s, float *flux, uint8_t *i
     or_collision_types(W, H, word, h, offx, offy, &st->kernel, bm);
     float *hn = (float *)malloc(N * sizeof(float));
     uint8_t *idn = (uint8_t *)malloc(N);
-    or_resolve(W, H, id, h, word, offx, offy, bm, div_bitmap, st, seed, *iteration, hn, idn, acc);
+    if (st->step.upliftMode == TECTO_UPLIFT_REFERENCE) {
+        float *uh = (float *)calloc(N, sizeof(float));
+        uint8_t *ut = (uint8_t *)calloc(N, 1);
+        or_resolve_ex(W, H, id, h, word, offx, offy, bm, div_bitmap, st, seed, *iteration, hn, idn, acc, uh, ut);
+        or_uplift_ref(W, H, word, uh, ut, h, plates, idn, hn, &st->kernel, NULL, NULL);
+        free(uh);
+        free(ut);
+    } else {
+        or_resolve(W, H, id, h, word, offx, offy, bm, div_bitmap, st, seed, *iteration, hn, idn, acc);
+    }
     memcpy(h, hn, N * sizeof(float));
     memcpy(id, idn, N);
     free(hn);

@@ -50,6 +50,18 @@ void or_resolve(int W, int H, const uint8_t *id_old, const float *h_old, const u
                 float *h_new, uint8_t *id_new, uint8_t *acc);
 
 /* Thermal erosion, `iters` gather iterations, in place. */
+void or_resolve_ex(int W, int H, const uint8_t *id_old, const float *h_old, const uint32_t *word,
+                   const int32_t *off_x, const int32_t *off_y, const uint8_t *bm, uint32_t *div_bitmap,
+                   const tecto_settings *st, uint32_t seed, uint32_t iteration, float *h_new,
+                   uint8_t *id_new, uint8_t *acc, float *up_h, uint8_t *up_t);
+
+/* The reference uplift (continental propagation, JFA distance field, applyUplift). */
+void or_uplift_ref(int W, int H, const uint32_t *word, const float *up_h, const uint8_t *up_t,
+                   const float *h_old, const tecto_plate *plates, const uint8_t *id_new, float *h_new,
+                   const tecto_kernel_settings *ks, int32_t *jfa_seed, int32_t *jfa_dist);
+float or_expf(float x);
+float or_log10f(float x);
+
 void or_thermal(int W, int H, float *h, int iters, const tecto_kernel_settings *ks);
 
 /* Hydraulic erosion, `iters` sub-iterations of step dt, in place; flux is 4 floats per cell. */

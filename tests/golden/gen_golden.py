@@ -95,6 +95,55 @@ def ref_step_composition(name, W, H, plates, vel, seed, kind, steps, hyd_iters, 
           "typed pairs", int((bm != 0).sum()))
 
 
+def ref_uplift_steps(name, W, H, plates, vel, seed, steps, prop_threshold):
+    """The reference uplift (continental propagation, JFA distance field, applyUplift) after each
+    of `steps` steps of the reference's collision kernels, in the reference's height units; the
+    propagation threshold is lowered so that the continental ray march takes several cells."""
+    R = O.ref()
+    st = ref_settings("reference")
+    st.kernel.continentalPropThreshold = prop_threshold
+    R.ref_set_settings(C.addressof(st.kernel))
+    h, ids, pl = world(W, H, plates, vel, seed, "reference")
+    N = W * H
+    bm = np.zeros(T.NUM_PAIRS, np.uint8)
+    div = np.zeros(T.NUM_DIV_WORDS, np.uint32)
+    wseed = 1000
+    rec = {}
+    for it in range(steps):
+        dest = np.zeros(N, np.uint32)
+        R.ref_pixel_movements(W, H, P(ids), P(pl), P(dest))
+        word = np.zeros(N, np.uint32)
+        R.ref_register_collisions(W, H, P(ids), P(dest), P(word))
+        R.ref_collision_types(W, H, P(ids), P(h), P(word), P(pl), P(bm))
+        hn = np.zeros_like(h)
+        idn = np.zeros_like(ids)
+        acc = np.zeros_like(ids)
+        uh = np.zeros_like(h)
+        ut = np.zeros_like(ids)
+        R.ref_process_collisions(W, H, P(ids), P(h), P(word), P(pl), P(bm), P(div), wseed, it,
+                                 P(hn), P(idn), P(acc), P(uh), P(ut))
+        h_res = hn.copy()
+        seeds = np.zeros((H, W), np.int32)
+        dists = np.zeros((H, W), np.int32)
+        R.ref_uplift(W, H, P(word), P(uh), P(ut), P(h), P(pl), P(idn), P(hn), P(seeds), P(dists))
+        for k, v in dict(word=word.reshape(H, W), up_h=uh, up_t=ut, h_old=h.copy(), plates=pl.copy(),
+                         id_new=idn.copy(), h_res=h_res, h_up=hn.copy(), seed=seeds, dist=dists,
+                         id_old=ids.copy(), bitmap=bm.copy(), div=div.copy()).items():
+            rec[f"{k}_{it}"] = v
+        R.ref_accretion(W, H, P(hn), P(acc), P(idn))
+        cx = pl["pixelCenter_x"] + pl["direction_x"] * pl["velocity"]
+        cy = pl["pixelCenter_y"] + pl["direction_y"] * pl["velocity"]
+        pl["pixelCenter_x"] = cx - np.floor(cx)
+        pl["pixelCenter_y"] = cy - np.floor(cy)
+        h, ids = hn, idn
+    np.savez_compressed(OUT / f"{name}.npz", W=W, H=H, steps=steps, seed=wseed,
+                        prop_threshold=np.float32(prop_threshold), **rec)
+    changed = sum(int((rec[f"h_up_{i}"] != rec[f"h_res_{i}"]).sum()) for i in range(steps))
+    seeded = sum(int((rec[f"seed_{i}"] >= 0).sum()) for i in range(steps))
+    cont = sum(int(((rec[f"up_t_{i}"] & 1) == 1).sum()) for i in range(steps))
+    print("wrote", name, "uplifted cells", changed, "cells with a seed", seeded, "continental records", cont)
+
+
 def ref_thermal_isolated(name, W, H, seed):
     """Thermal on isolated peaks (4 cells apart) with the reference's own parameters (talus
     threshold 0.5 * 1000 m, amplitude 0.5 m): a neighbour receives at most 0.5 m and never becomes
@@ -155,6 +204,7 @@ def main():
     ref_step_composition("ref_steps_baseline_64x64", 64, 64, 8, 1.0, 7, "baseline", 6, 20, 0.02)
     ref_step_composition("ref_steps_baseline_128x48", 128, 48, 5, 1.0, 3, "baseline", 6, 20, 0.02)
     ref_step_composition("ref_steps_reference_64x64", 64, 64, 8, 1.0, 9, "reference", 6, 10, 1.0)
+    ref_uplift_steps("ref_uplift_64x48", 64, 48, 8, 1.5, 21, 5, 12000.0)
     ref_thermal_isolated("ref_thermal_isolated_64x64", 64, 64, 13)
     ref_ccl_cases("ref_ccl_cases")
 
