@@ -184,7 +184,10 @@ typedef struct tecto_plate {
 #define TECTO_FIELD_SORT_KEYS 9    /* u32[W*H]  destination cells of the last step, sorted */
 #define TECTO_FIELD_SORT_VALS 10   /* u32[W*H]  source cells, in the same order */
 #define TECTO_FIELD_ACCRETION 11   /* u8[W*H]   accretion marks of the last resolve (0 = none) */
-#define TECTO_FIELD_COUNT 12
+#define TECTO_FIELD_JFA_SEED 12    /* i32[W*H]  reference uplift of the last step: nearest propagated
+                                      collision cell (JFA seed), -1 none (read only) */
+#define TECTO_FIELD_JFA_DIST 13    /* i32[W*H]  its distance in whole cells (JFAComputeDistance), -1 none */
+#define TECTO_FIELD_COUNT 14
 
 /* ---- world lifecycle (replaces PlateTectonicSim, plate_tectonic_sim.h:110-130) ------ */
 

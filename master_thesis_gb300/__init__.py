@@ -36,7 +36,7 @@ CCL_4, CCL_8, CCL_REF8 = 4, 8, 9
 
 (FIELD_HEIGHT, FIELD_WATER, FIELD_SEDIMENT, FIELD_FLUX, FIELD_PLATE_ID, FIELD_LABELS,
  FIELD_COLLISION, FIELD_TYPE_BITMAP, FIELD_DIV_BITMAP, FIELD_SORT_KEYS, FIELD_SORT_VALS,
- FIELD_ACCRETION) = range(12)
+ FIELD_ACCRETION, FIELD_JFA_SEED, FIELD_JFA_DIST) = range(14)
 
 KERNEL_FIELDS = [
     ("inelasticCollisionMultiplierContinental", C.c_float),
@@ -319,7 +319,7 @@ _FIELD_DT = {
     FIELD_HEIGHT: (np.float32, 1), FIELD_WATER: (np.float32, 1), FIELD_SEDIMENT: (np.float32, 1),
     FIELD_FLUX: (np.float32, 4), FIELD_PLATE_ID: (np.uint8, 1), FIELD_LABELS: (np.uint32, 1),
     FIELD_COLLISION: (np.uint32, 1), FIELD_SORT_KEYS: (np.uint32, 1), FIELD_SORT_VALS: (np.uint32, 1),
-    FIELD_ACCRETION: (np.uint8, 1),
+    FIELD_ACCRETION: (np.uint8, 1), FIELD_JFA_SEED: (np.int32, 1), FIELD_JFA_DIST: (np.int32, 1),
 }
 
 

@@ -22,6 +22,7 @@ SOURCES = [
     "tecto_batch.cu",
     "tecto_server.cu",
     "tecto_tune.cu",
+    "k_uplift.cu",
     "k_sort.cu",
     "k_sort_noalloc.cu",
     "k_collide.cu",

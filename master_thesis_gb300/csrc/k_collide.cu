@@ -7,14 +7,16 @@ namespace tecto {
 namespace {
 
 // Per-plate integer displacement (getPixelMovements, :248-257) and the sub-cell centre update
-// of applyPlateMovementChanges (:1871-1878), one block per world.  Also resets the world's
-// per-step accretion list.
+// of applyPlateMovementChanges (:1871-1878), one block per world; the record before the update is
+// kept in plates_prev for the kernels of the same step.  Also resets the world's per-step
+// accretion list.
 __global__ void k_plates(const WorldDev *worlds)
 {
     const WorldDev &wd = worlds[blockIdx.x];
     const int k = threadIdx.x;
     if (k < kPlates) {
         tecto_plate p = wd.plates[k];
+        wd.plates_prev[k] = p;  // the record the rest of the step sees in the reference
         const float mx = p.direction_x * p.velocity;
         const float my = p.direction_y * p.velocity;
         const float cx = p.pixelCenter_x + mx;

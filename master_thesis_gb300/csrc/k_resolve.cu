@@ -20,6 +20,8 @@ struct ResolveParams {
     float tmin, tmax, tfac;
     float amount;
     float wts[2 * kMaxBlurRadius + 1];
+    float *upl_h;      // reference uplift: processConvergence's records by virtual cell, or null
+    uint8_t *upl_t;
 };
 
 // One world's view inside the resolve kernel.
@@ -71,6 +73,8 @@ __device__ __forceinline__ float resolve_cell(const ResolveParams &p, const Reso
                                               const int2 *s_off, int x, int y, uint32_t d, uint32_t cv,
                                               uint32_t seed, uint32_t iteration, uint8_t *id_out)
 {
+    // Convergent cells also leave processConvergence's UpliftData (:501-582) for the reference
+    // uplift when it is on: heightAddition, the sum of each owner pair's lower height, and typeByte.
     const int W = w.W, H = w.H;
     if (cv == 0u) {
         // processDivergence (:301-362)
@@ -122,13 +126,24 @@ __device__ __forceinline__ float resolve_cell(const ResolveParams &p, const Reso
         if (!sub[i]) owner = i;
     const uint8_t ownerId = ids[owner];
     float writeH = heights[owner];
+    float hadd = 0.0f;
+    uint32_t tbyte = 0;
     for (int a = 0; a < pairLen; ++a) {
         const int ia = PA[a], ib = PB[a];
         float hh;
         if (ia == owner) hh = heights[ib];
         else if (ib == owner) hh = heights[ia];
         else continue;
-        if (hh > writeH) writeH = hh;  // writeHeight keeps the larger of the pair
+        if (hh > writeH) {  // writeHeight keeps the larger of the pair, the sum the smaller
+            const float tmp = hh;
+            hh = writeH;
+            writeH = tmp;
+        }
+        hadd = hadd + hh;
+        if (ia == owner)
+            tbyte |= (types[a] == 2u ? 0u : 1u) | ((uint32_t)(ia & 3) << 1) | ((uint32_t)(ib & 3) << 3);
+        else
+            tbyte |= (types[a] == 1u ? 0u : 1u) | ((uint32_t)(ib & 3) << 1) | ((uint32_t)(ia & 3) << 3);
         int other = -1;
         if (ia == owner && types[a] == 4u) other = ib;
         else if (ib == owner && types[a] == 3u) other = ia;
@@ -143,6 +158,10 @@ __device__ __forceinline__ float resolve_cell(const ResolveParams &p, const Reso
             }
             mark_accretion(p, w, target, d, ownerId);
         }
+    }
+    if (p.upl_h) {
+        p.upl_h[w.vbase + d] = hadd;
+        p.upl_t[w.vbase + d] = (uint8_t)tbyte;
     }
     *id_out = ownerId;
     return writeH;
@@ -286,6 +305,14 @@ int launch_resolve(Batch &b, cudaStream_t st)
     p.tmax = s.kernel.divergence_height_target_max;
     p.tfac = s.kernel.divergence_interpolation_factor;
     p.amount = s.step.upliftAmount;
+    if (s.step.upliftMode == TECTO_UPLIFT_REFERENCE) {
+        p.upl_h = b.upref.upl_h;
+        p.upl_t = b.upref.upl_t;
+        if (!p.upl_h) {
+            set_error("reference uplift scratch not prepared");
+            return TECTO_ERR_INVALID;
+        }
+    }
     int R = 0;
     if (s.step.upliftMode == TECTO_UPLIFT_GAUSSIAN) {
         R = s.step.upliftRadius;

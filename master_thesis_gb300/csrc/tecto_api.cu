@@ -113,6 +113,12 @@ void field_info(tecto_world *w, int field, void **ptr, size_t *bytes)
             if (w->own && w->own->arena) { *ptr = w->own->vals[w->own->sort_final]; *bytes = N * 4; }
             break;
         case TECTO_FIELD_ACCRETION: *ptr = d.acc_u8; *bytes = N; break;
+        case TECTO_FIELD_JFA_SEED:
+            if (w->own && w->own->upref.arena) { *ptr = w->own->upref.jfa[w->own->upref_final]; *bytes = N * 4; }
+            break;
+        case TECTO_FIELD_JFA_DIST:
+            if (w->own && w->own->upref.arena) { *ptr = w->own->upref.dist; *bytes = N * 4; }
+            break;
         default: break;
     }
 }
@@ -137,7 +143,8 @@ size_t world_footprint(int W, int H)
     L.add(N * 16); L.add(N * 16); L.add(N); L.add(N);
     L.add(N * 4); L.add(N * 4); L.add(N * 4); L.add(N * 8); L.add(N * 4); L.add(N * 8); L.add(N * 4); L.add(N);
     L.add(kPairs); L.add(kDivWords * 4); L.add(kDivWords * 4); L.add(kPairs * sizeof(PairCounts));
-    L.add(kPlates * sizeof(tecto_plate)); L.add((kPlates + 1) * sizeof(int2)); L.add(sizeof(Control));
+    L.add(kPlates * sizeof(tecto_plate)); L.add(kPlates * sizeof(tecto_plate));
+    L.add((kPlates + 1) * sizeof(int2)); L.add(sizeof(Control));
     // its share of a batch's sort: key/value ping-pong plus the scratch of the widest digit choice
     size_t scratch = 0;
     for (int rb = 8; rb <= kMaxRadixBits; ++rb)
@@ -201,6 +208,7 @@ int tecto_world_create(const tecto_settings *settings, int width, int height, ui
     const size_t o_hd = L.add(kDivWords * 4);
     const size_t o_cnt = L.add(kPairs * sizeof(PairCounts));
     const size_t o_pl = L.add(kPlates * sizeof(tecto_plate));
+    const size_t o_plp = L.add(kPlates * sizeof(tecto_plate));
     const size_t o_off = L.add((kPlates + 1) * sizeof(int2));
     const size_t o_ctl = L.add(sizeof(Control));
     cudaError_t e = cudaMalloc(&w->arena, L.total);
@@ -238,6 +246,7 @@ int tecto_world_create(const tecto_settings *settings, int width, int height, ui
     d.has_div = (uint32_t *)(base + o_hd);
     d.counts = (PairCounts *)(base + o_cnt);
     d.plates = (tecto_plate *)(base + o_pl);
+    d.plates_prev = (tecto_plate *)(base + o_plp);
     d.off = (int2 *)(base + o_off);
     d.ctl = (Control *)(base + o_ctl);
     e = cudaMemset(w->arena, 0, L.total);
@@ -621,6 +630,7 @@ int tecto_phase_resolve(tecto_world *w, tecto_stream_t stream)
 {
     TECTO_PHASE_PROLOGUE
     rc = launch_resolve(*b, st);
+    if (rc == TECTO_OK && b->settings.step.upliftMode == TECTO_UPLIFT_REFERENCE) rc = launch_uplift_ref(*b, st);
     TECTO_PHASE_EPILOGUE
 }
 
@@ -694,6 +704,10 @@ int tecto_world_check(tecto_world *w, tecto_stream_t stream)
     if (err[0] | err[1]) {
         cudaMemset(&w->dev.ctl->error, 0, 4);
         if (w->own && w->own->sort.error) cudaMemset(w->own->sort.error, 0, 4);
+        if ((err[0] & kErrUpliftCapacity) && !((err[0] & ~kErrUpliftCapacity) | err[1])) {
+            set_error("reference uplift: more propagation events than its scratch holds");
+            return TECTO_ERR_UNSUPPORTED;
+        }
         set_error("a bounded device-side wait gave up");
         return TECTO_ERR_DEVICE_TIMEOUT;
     }

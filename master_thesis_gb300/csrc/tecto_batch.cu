@@ -106,6 +106,7 @@ int batch_leave(Batch &b, tecto_world *w)
 void batch_release(Batch &b)
 {
     drop_graphs(b);
+    uplift_ref_release(b);
     if (b.table_arena) cudaFree(b.table_arena);
     if (b.arena) cudaFree(b.arena);
     b.table_arena = nullptr;
@@ -223,6 +224,7 @@ int batch_prepare(Batch &b, cudaStream_t st)
         char *q = (char *)b.arena + 4 * a256(b.capacity * 4) + a256(sizeof(BatchCtl));
         sort_scratch_carve(q, total, kb, rb, &b.sort);
     }
+    if ((rc = uplift_ref_prepare(b, st)) != TECTO_OK) return rc;
     // the error word may now sit where a larger batch kept look-back status words
     TECTO_CUDA(cudaMemsetAsync(b.sort.error, 0, 4, st));
     TECTO_CUDA(cudaStreamSynchronize(st));
@@ -240,6 +242,7 @@ int batch_enqueue_step(Batch &b, cudaStream_t st, int ccl)
     if ((rc = launch_words(b, st)) != TECTO_OK) return rc;
     if ((rc = launch_type_matrix(b, st)) != TECTO_OK) return rc;
     if ((rc = launch_resolve(b, st)) != TECTO_OK) return rc;
+    if (s.step.upliftMode == TECTO_UPLIFT_REFERENCE && (rc = launch_uplift_ref(b, st)) != TECTO_OK) return rc;
     if ((rc = launch_thermal(b, s.step.thermalIterations, st)) != TECTO_OK) return rc;
     if ((rc = launch_hydraulic(b, s.step.hydraulicIterations, s.step.hydraulicDt, st)) != TECTO_OK) return rc;
     if ((rc = launch_finish(b, st)) != TECTO_OK) return rc;

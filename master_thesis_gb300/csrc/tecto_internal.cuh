@@ -35,6 +35,7 @@ constexpr uint32_t kSpinLimit = 1u << 24;       // bounded waits: give up, flag,
 
 // Device error flag bits.
 constexpr uint32_t kErrLookbackTimeout = 1u;
+constexpr uint32_t kErrUpliftCapacity = 2u;    // reference uplift: more bucket entries than its scratch holds
 
 // Per-pair collision evidence, CollisionTypeCounts field order
 // (src/cuda_compute/plate_tectonics_kernel.cuh:47-54).
@@ -93,8 +94,29 @@ struct WorldDev {
     uint32_t *has_div;      // [kDivWords]
     PairCounts *counts;     // [kPairs]
     tecto_plate *plates;    // [kPlates]
+    tecto_plate *plates_prev;  // [kPlates] plate records before this step's centre update
     int2 *off;              // [kPlates + 1] this step's integer displacement per plate
     Control *ctl;
+};
+
+// Batch-level scratch of the reference uplift (TECTO_UPLIFT_REFERENCE), indexed by virtual cell.
+struct UpliftRefScratch {
+    size_t cells = 0;       // capacity in cells
+    size_t ecap = 0;        // capacity in bucket entries
+    void *arena = nullptr;
+    float *upl_h = nullptr;       // processConvergence's heightAddition (convergent cells)
+    uint8_t *upl_t = nullptr;     // processConvergence's typeByte
+    uint32_t *cnt = nullptr;      // entries per target cell, then fill cursor
+    uint32_t *off = nullptr;      // first entry of each target cell
+    uint32_t *blk = nullptr;      // scan block totals
+    uint32_t *succ = nullptr;     // per source: bit (2k + j) set when its insert event succeeded
+    float *prop_h = nullptr;      // PropagatedUpliftData, structure of arrays
+    uint32_t *prop_inv = nullptr;
+    uint8_t *prop_t = nullptr;
+    int32_t *jfa[2] = {};         // nearest seed (world-local cell index) or -1
+    int32_t *dist = nullptr;      // JFAComputeDistance: distance to the seed, -1 none
+    uint32_t *ent_key = nullptr;  // bucket entries: (source virtual cell << 3) | slot
+    uint32_t *ent_val = nullptr;  // payload: plate pair, or a contribution's bits
 };
 
 // Phase work lists.
@@ -129,6 +151,8 @@ struct Batch {
     size_t arena_bytes = 0;
     BatchCtl *bctl = nullptr;
     SortScratch sort{};
+    UpliftRefScratch upref{};
+    int upref_final = 0;                     // jfa[] half holding the last step's seeds
     // graphs of one step keyed by (cur_h, cur_wsf, cur_id, ccl)
     cudaGraphExec_t graphs[16] = {};
     bool graph_valid[16] = {};
@@ -243,6 +267,9 @@ int launch_clear_marks(Batch &b, cudaStream_t st);
 int launch_bump_iteration(Batch &b, cudaStream_t st);
 // due_only: skip worlds whose step counter is not a multiple of iterationsForCCL
 int launch_ccl(Batch &b, int connectivity, bool due_only, cudaStream_t st);
+int launch_uplift_ref(Batch &b, cudaStream_t st);          // k_uplift.cu, after launch_resolve
+int uplift_ref_prepare(Batch &b, cudaStream_t st);         // allocate the scratch when the mode needs it
+void uplift_ref_release(Batch &b);
 void gaussian_weights(float sigma, int radius, float *out);
 int ensure_kernel_attributes();
 int hydro_variant_for(const tecto_settings &s);  // 0 when the settings leave the choice open
