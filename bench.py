@@ -463,6 +463,47 @@ def engine_extras(args, T, torch, stream, s, specs, total, batched_value):
     return out
 
 
+def run_case(args):
+    """Small fixed workloads for ncu captures (no timing, no JSON line):
+    erosion2048  one 5-iteration thermal launch and one fused hydraulic launch on a 2048^2 world;
+    plain2048    4 steps of one 2048^2 world, 32 plates;
+    batch        the mixed-size batch with the default tile and digit width, 4 steps."""
+    import torch
+
+    import master_thesis_gb300 as T
+
+    stream = torch.cuda.Stream()
+    s = T.baseline_settings()
+    if args.case == "erosion2048":
+        w = T.World(s, 2048, 2048, seed=1000)
+        w.init_synthetic_device(32, 1.0, 1)
+        rng = np.random.default_rng(1)
+        w.upload(T.FIELD_WATER, np.abs(rng.normal(0, 0.05, (2048, 2048))).astype(np.float32))
+        w.upload(T.FIELD_SEDIMENT, np.abs(rng.normal(0, 0.01, (2048, 2048))).astype(np.float32))
+        w.thermal(5, stream)
+        w.hydraulic(1, s.step.hydraulicDt, stream)
+        w.check(stream)
+    elif args.case == "plain2048":
+        w = T.World(s, 2048, 2048, seed=1000)
+        w.init_synthetic_device(32, 1.0, 1)
+        w.step(4, stream)
+        w.check(stream)
+    else:
+        s.step.hydraulicTile = 4
+        s.step.sortRadixBits = 9
+        b = T.Batch()
+        worlds = []
+        for W, H, P, gs, wsd in mixed_worlds():
+            w = T.World(s, W, H, seed=wsd)
+            w.init_synthetic_device(P, 1.0, gs)
+            b.add(w, stream)
+            worlds.append(w)
+        b.step(4, stream)
+        b.check(stream)
+    stream.synchronize()
+    print("case", args.case, "ok")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -471,10 +512,13 @@ def main():
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
     ap.add_argument("--serve-requests", type=int, default=40)
     ap.add_argument("--quick", action="store_true", help="headline only (no plain/served/large-world lines)")
+    ap.add_argument("--case", choices=["erosion2048", "plain2048", "batch"], help="a small fixed workload for profilers")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_setup()
-    if args.impl == "reference":
+    if args.case:
+        run_case(args)
+    elif args.impl == "reference":
         run_reference(args, ws, rank)
     else:
         run_engine(args, ws, rank, local)
