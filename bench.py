@@ -205,6 +205,7 @@ def run_reference(args, ws, rank):
         cells += c
         rates.append(r)
     rate = cells / secs
+    ref_gpu = reference_gpu_lines(s)
     line = {
         "metric": "cell_updates_per_s", "value": rate, "unit": "cell-updates/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
@@ -217,8 +218,50 @@ def run_reference(args, ws, rank):
                          "sample": f"{worlds} world-steps of the mixed-size batch ({cells} cell-updates, "
                                    f"{secs:.1f} s of stepping) on {cores} OpenMP threads"},
         "e2e": {"value": rate, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "reference_gpu": ref_gpu,
     }
     print(json.dumps(line), flush=True)
+
+
+def reference_gpu_lines(s):
+    """The reference's own CUDA kernels on this GPU (oracle/refgpu/ref_gpu_harness.cpp), one world
+    at a time, at 2048^2 (32 plates) and 8192^2 (64 plates, velocities in [-2, 2], 8-connected CCL
+    every step)."""
+    try:
+        import torch
+
+        if not torch.cuda.is_available():
+            return {"unavailable": "no CUDA GPU"}
+        import master_thesis_gb300 as T
+        import oracle as O
+    except Exception as e:  # noqa: BLE001
+        return {"unavailable": f"{type(e).__name__}: {e}"}
+    out = {"kernels": "getPixelMovements, registerPlateCollisions, determineCollisionType, "
+                      "createCollisionTypeMatrix, thermalErosionKernel x thermal iterations, rain/flux/flow/"
+                      "sediment/transport/evaporate + 2 copies x hydraulic iterations, copies back, "
+                      "applyAccretion, CCL when due; processCollisions not launched (reads past a local "
+                      "array), a height copy stands in for it",
+           "launch": "256 threads per block, one thread per cell, one stream, no per-launch synchronisation"}
+    # the reference's kernels print diagnostics from the device; keep them off stdout, which
+    # carries the JSON line
+    sys.stdout.flush()
+    saved = os.dup(1)
+    os.dup2(2, 1)
+    try:
+        for name, W, P, vel, ccl_every in (("2048", 2048, 32, 1.0, 10), ("8192", 8192, 64, 2.0, 1)):
+            try:
+                h, ids, pl = T.generate_world(W, W, P, vel, 1)
+                st = T.baseline_settings()
+                st.sim.iterationsForCCL = ccl_every
+                ms = O.ref_gpu_time(W, W, h, ids, pl, st, steps=5 if W <= 2048 else 3, warmup=2)
+                out[name] = {"value": W * W / (ms / 1e3), "unit": "cell-updates/s", "ms_per_step": ms}
+            except Exception as e:  # noqa: BLE001
+                out[name] = {"unavailable": f"{type(e).__name__}: {e}"}
+        torch.cuda.synchronize()
+    finally:
+        os.dup2(saved, 1)
+        os.close(saved)
+    return out
 
 
 def event_ms(torch, stream, fn):

@@ -2,7 +2,7 @@
 to the reference's own kernels compiled for the CPU (oracle/_ref/libtecto_ref.so).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and bench.py's CPU
-baseline leg; never by the engine.
+baseline and reference legs; never by the engine.
 """
 from __future__ import annotations
 
@@ -21,9 +21,37 @@ _r = None
 
 
 def build(ref: bool = False) -> None:
-    """make the oracle (and, with ref=True, the reference-on-CPU library)."""
-    targets = ["all"] + (["ref"] if ref else [])
+    """make the oracle and the reference-GPU timing harness (and, with ref=True, the
+    reference-on-CPU library and the reference's device code for the GPU)."""
+    targets = ["all", "harness"] + (["ref", "refgpu"] if ref else [])
     subprocess.run(["make", "-s", "-C", str(HERE), *targets], check=True)
+
+
+REF_CUBIN = HERE / "_ref" / "ref_kernels.cubin"
+REF_GPU_LIB = HERE / "_build" / "libref_gpu.so"
+
+
+def ref_gpu_time(W, H, h, ids, plates, settings, steps=5, warmup=2):
+    """Milliseconds per step of the reference's own CUDA kernels (refgpu/ref_gpu_harness.cpp) on
+    this GPU for the world (h, ids, plates) with `settings` (benchmark physics mapped onto the
+    reference's parameters); raises RuntimeError when the cubin or the GPU is unavailable."""
+    if not REF_CUBIN.exists():
+        raise RuntimeError("the reference's device code was not built (oracle/_ref/ref_kernels.cubin is absent)")
+    L = C.CDLL(str(REF_GPU_LIB))
+    L.refgpu_error.restype = C.c_char_p
+    L.refgpu_load.argtypes = [C.c_char_p]
+    L.refgpu_time_steps.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                    C.c_float, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)]
+    if L.refgpu_load(str(REF_CUBIN).encode()) != 0:
+        raise RuntimeError(L.refgpu_error().decode())
+    ms = C.c_double()
+    rc = L.refgpu_time_steps(W, H, _P(h), _P(ids), _P(plates), C.addressof(settings.kernel),
+                             settings.step.hydraulicIterations, settings.step.hydraulicDt,
+                             settings.step.thermalIterations, settings.sim.iterationsForCCL, steps, warmup,
+                             C.byref(ms))
+    if rc != 0:
+        raise RuntimeError(L.refgpu_error().decode())
+    return ms.value
 
 
 def _P(a):
