@@ -134,7 +134,8 @@ typedef struct tecto_step_settings {
     int cclConnectivity;      /* TECTO_CCL_* */
     int sortRadixBits;        /* collision sort digit width 8..11; 0 = autotuner's choice, else 8 */
     int hydraulicTile;        /* 0 = autotuner's choice, else 4; 1: 64x16/256 threads, 2: 64x32/256,
-                                 3: 64x32/512, 4: 64x32/1024, 5: 64x64/1024 */
+                                 3: 64x32/512, 4: 64x32/1024, 5: 64x64/1024, 6: 64x16/512 (3 blocks
+                                 per SM), 7: 64x16/384 (4 blocks per SM) */
     int reserved[6];
 } tecto_step_settings;
 
@@ -325,9 +326,9 @@ int tecto_batch_phase_thermal(tecto_batch *batch, int iterations, tecto_stream_t
  * hydraulicTile / sortRadixBits at 0 use the choice cached for their class, else for the nearest
  * tuned class on their device, else the defaults (variant 4, 8-bit digits). */
 typedef struct tecto_tuning {
-    int hydraulicTile;       /* chosen variant, 1..5 */
+    int hydraulicTile;       /* chosen variant, 1..7 */
     int sortRadixBits;       /* chosen digit width, 8..11 */
-    float hydraulic_ms[5];   /* one hydraulic sub-iteration with variant 1..5 */
+    float hydraulic_ms[7];   /* one hydraulic sub-iteration with variant 1..7 */
     float sort_ms[4];        /* the collision sort with 8..11-bit digits */
 } tecto_tuning;
 int tecto_autotune(const tecto_settings *settings, const int *widths, const int *heights, int count,

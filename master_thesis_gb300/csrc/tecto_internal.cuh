@@ -274,7 +274,7 @@ void gaussian_weights(float sigma, int radius, float *out);
 int ensure_kernel_attributes();
 int hydro_variant_for(const tecto_settings &s);  // 0 when the settings leave the choice open
 constexpr int kDefaultRadixBits = 8;
-constexpr int kHydroVariantCount = 5;
+constexpr int kHydroVariantCount = 7;
 constexpr int kDefaultHydroVariant = 4;          // 64 x 32 cells, 1024 threads
 
 // Autotuner cache (tecto_tune.cu): best hydraulic tile variant and sort digit width for a batch

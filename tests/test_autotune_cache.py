@@ -39,7 +39,7 @@ def test_later_record_replaces():
     assert T.autotune_lookup(0, 1 << 22, 1) == (5, 10)
 
 
-@pytest.mark.parametrize("args", [(0, 1 << 20, 1, 0, 8), (0, 1 << 20, 1, 6, 8), (0, 1 << 20, 1, 4, 7),
+@pytest.mark.parametrize("args", [(0, 1 << 20, 1, 0, 8), (0, 1 << 20, 1, 8, 8), (0, 1 << 20, 1, 4, 7),
                                   (0, 1 << 20, 1, 4, 12), (0, 0, 1, 4, 8), (0, 1 << 20, 0, 4, 8),
                                   (-1, 1 << 20, 1, 4, 8)])
 def test_invalid_records_rejected(args):

@@ -113,7 +113,7 @@ def test_phases_match_oracle(kind, W, H):
     print(kind, W, H, {k: max(v) for k, v in report.items()})
 
 
-@pytest.mark.parametrize("tile", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("tile", [1, 2, 3, 4, 5, 6, 7])
 @pytest.mark.parametrize("W,H,dt", [(100, 60, 0.02), (33, 17, 0.02), (300, 200, 0.02), (128, 96, 1.0)])
 def test_hydraulic_tile_variants_match_oracle(tile, W, H, dt):
     """Every hydraulic tile shape (interior tiles without wrap, edge tiles with it) gives the
