@@ -136,7 +136,11 @@ typedef struct tecto_step_settings {
     int hydraulicTile;        /* 0 = autotuner's choice, else 4; 1: 64x16/256 threads, 2: 64x32/256,
                                  3: 64x32/512, 4: 64x32/1024, 5: 64x64/1024, 6: 64x16/512 (3 blocks
                                  per SM), 7: 64x16/384 (4 blocks per SM) */
-    int reserved[6];
+    int thermalTile;          /* 0 = autotuner's choice, else 4; 1: 64x32 tiles / 1024 threads, up to 5
+                                 iterations per launch; 2: 64x16 / 512, 2 blocks per SM, up to 4;
+                                 3: 64x16 / 768, 2 blocks per SM, up to 3; 4: 64x16 / 512, 3 blocks
+                                 per SM, up to 2 */
+    int reserved[5];
 } tecto_step_settings;
 
 typedef struct tecto_settings {
@@ -319,17 +323,21 @@ int tecto_batch_phase_thermal(tecto_batch *batch, int iterations, tecto_stream_t
 /* ---- autotuner ---------------------------------------------------------------------------
  *
  * No counterpart in the reference (fixed launch shapes, plate_tectonic_sim.cu).  Times every
- * hydraulic tile variant (one sub-iteration) and every sort digit width (the collision sort) on
- * scratch worlds of the given shapes with synthetic content, and returns the fastest of each.
+ * hydraulic tile variant (one sub-iteration), every thermal tile variant (ten iterations) and every
+ * sort digit width (the collision sort) on scratch worlds of the given shapes with synthetic
+ * content, and returns the fastest of each.
  * The caller's worlds are not touched.  The choice is cached per device and batch shape class
  * (total cells and mean world cells, half-octave classes); batches whose settings leave
- * hydraulicTile / sortRadixBits at 0 use the choice cached for their class, else for the nearest
- * tuned class on their device, else the defaults (variant 4, 8-bit digits). */
+ * hydraulicTile / thermalTile / sortRadixBits at 0 use the choice cached for their class, else for
+ * the nearest tuned class on their device, else the defaults (hydraulic variant 4, thermal
+ * variant 4, 8-bit digits). */
 typedef struct tecto_tuning {
     int hydraulicTile;       /* chosen variant, 1..7 */
     int sortRadixBits;       /* chosen digit width, 8..11 */
+    int thermalTile;         /* chosen variant, 1..4 */
     float hydraulic_ms[7];   /* one hydraulic sub-iteration with variant 1..7 */
     float sort_ms[4];        /* the collision sort with 8..11-bit digits */
+    float thermal_ms[4];     /* ten thermal iterations with variant 1..4 */
 } tecto_tuning;
 int tecto_autotune(const tecto_settings *settings, const int *widths, const int *heights, int count,
                    tecto_stream_t stream, tecto_tuning *out);
@@ -338,8 +346,10 @@ int tecto_batch_autotune(tecto_batch *batch, tecto_stream_t stream, tecto_tuning
 /* Tune for one world's shape and apply the choice to its plain stepping. */
 int tecto_world_autotune(tecto_world *world, tecto_stream_t stream, tecto_tuning *out);
 /* Cache access (no device work): record a choice for a class, look one up, clear the cache. */
-int tecto_autotune_record(int device, size_t total_cells, int worlds, int hydraulicTile, int sortRadixBits);
-int tecto_autotune_lookup(int device, size_t total_cells, int worlds, int *hydraulicTile, int *sortRadixBits);
+int tecto_autotune_record(int device, size_t total_cells, int worlds, int hydraulicTile, int sortRadixBits,
+                          int thermalTile);
+int tecto_autotune_lookup(int device, size_t total_cells, int worlds, int *hydraulicTile, int *sortRadixBits,
+                          int *thermalTile);
 int tecto_autotune_clear(void);
 
 /* Device bytes one world of width x height holds, including its share of batch buffers: the

@@ -119,7 +119,8 @@ class StepSettings(C.Structure):
         ("cclConnectivity", C.c_int),
         ("sortRadixBits", C.c_int),
         ("hydraulicTile", C.c_int),
-        ("reserved", C.c_int * 6),
+        ("thermalTile", C.c_int),
+        ("reserved", C.c_int * 5),
     ]
 
 
@@ -173,14 +174,16 @@ class ServerStats(C.Structure):
 class Tuning(C.Structure):
     """tecto_tuning: the autotuner's choice and the per-candidate timings."""
     _fields_ = [
-        ("hydraulicTile", C.c_int), ("sortRadixBits", C.c_int),
-        ("hydraulic_ms", C.c_float * 7), ("sort_ms", C.c_float * 4),
+        ("hydraulicTile", C.c_int), ("sortRadixBits", C.c_int), ("thermalTile", C.c_int),
+        ("hydraulic_ms", C.c_float * 7), ("sort_ms", C.c_float * 4), ("thermal_ms", C.c_float * 4),
     ]
 
     def as_dict(self) -> dict:
         return {"hydraulicTile": self.hydraulicTile, "sortRadixBits": self.sortRadixBits,
+                "thermalTile": self.thermalTile,
                 "hydraulic_ms": [round(x, 4) for x in self.hydraulic_ms],
-                "sort_ms": [round(x, 4) for x in self.sort_ms]}
+                "sort_ms": [round(x, 4) for x in self.sort_ms],
+                "thermal_ms": [round(x, 4) for x in self.thermal_ms]}
 
 
 SERVER_DRY_RUN = 1
@@ -246,8 +249,9 @@ def _declare(L: C.CDLL) -> None:
         "tecto_autotune": ([C.POINTER(Settings), P, P, C.c_int, P, C.POINTER(Tuning)], C.c_int),
         "tecto_batch_autotune": ([P, P, C.POINTER(Tuning)], C.c_int),
         "tecto_world_autotune": ([P, P, C.POINTER(Tuning)], C.c_int),
-        "tecto_autotune_record": ([C.c_int, C.c_size_t, C.c_int, C.c_int, C.c_int], C.c_int),
-        "tecto_autotune_lookup": ([C.c_int, C.c_size_t, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)], C.c_int),
+        "tecto_autotune_record": ([C.c_int, C.c_size_t, C.c_int, C.c_int, C.c_int, C.c_int], C.c_int),
+        "tecto_autotune_lookup": ([C.c_int, C.c_size_t, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                   C.POINTER(C.c_int)], C.c_int),
         "tecto_autotune_clear": ([], C.c_int),
         "tecto_server_create": ([C.POINTER(Settings), C.c_size_t, C.c_int, C.c_int, C.POINTER(P)], C.c_int),
         "tecto_server_destroy": ([P], C.c_int),
@@ -517,18 +521,20 @@ def autotune(settings: Settings, shapes, stream=None) -> Tuning:
     return t
 
 
-def autotune_record(device: int, total_cells: int, worlds: int, hydraulic_tile: int, radix_bits: int) -> None:
-    check(lib().tecto_autotune_record(device, total_cells, worlds, hydraulic_tile, radix_bits), "tecto_autotune_record")
+def autotune_record(device: int, total_cells: int, worlds: int, hydraulic_tile: int, radix_bits: int,
+                    thermal_tile: int = 3) -> None:
+    check(lib().tecto_autotune_record(device, total_cells, worlds, hydraulic_tile, radix_bits, thermal_tile),
+          "tecto_autotune_record")
 
 
 def autotune_lookup(device: int, total_cells: int, worlds: int):
-    """(hydraulicTile, sortRadixBits) cached for the class, or None."""
-    h, r = C.c_int(), C.c_int()
-    rc = lib().tecto_autotune_lookup(device, total_cells, worlds, C.byref(h), C.byref(r))
+    """(hydraulicTile, sortRadixBits, thermalTile) cached for the class, or None."""
+    h, r, t = C.c_int(), C.c_int(), C.c_int()
+    rc = lib().tecto_autotune_lookup(device, total_cells, worlds, C.byref(h), C.byref(r), C.byref(t))
     if rc == -7:
         return None
     check(rc, "tecto_autotune_lookup")
-    return h.value, r.value
+    return h.value, r.value, t.value
 
 
 def autotune_clear() -> None:

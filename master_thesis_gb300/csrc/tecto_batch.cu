@@ -24,7 +24,7 @@ void drop_graphs(Batch &b)
 void build_tiles(const Batch &b, int kind, std::vector<uint2> &out)
 {
     int tx = 0, ty = 0;
-    tile_extent(kind, b.hydro_variant, &tx, &ty);
+    tile_extent(kind, kind == TK_THERMAL ? b.thermal_variant : b.hydro_variant, &tx, &ty);
     out.clear();
     for (size_t wi = 0; wi < b.members.size(); ++wi) {
         const tecto_world *w = b.members[wi];
@@ -119,8 +119,10 @@ void batch_release(Batch &b)
 
 // Tile variant and digit width: explicit settings first, then the autotuner's choice for this
 // batch (or its cached choice for the shape class), then the defaults.
-static void choose_tuning(const Batch &b, int *variant, int *rb)
+static void choose_tuning(const Batch &b, int *variant, int *rb, int *tvariant)
 {
+    *tvariant = thermal_variant_for(b.settings);
+    if (*tvariant == 0) *tvariant = b.tuned_thermal ? b.tuned_thermal : kDefaultThermalVariant;
     *variant = hydro_variant_for(b.settings);
     if (*variant == 0) *variant = b.tuned_hydro ? b.tuned_hydro : kDefaultHydroVariant;
     *rb = b.settings.step.sortRadixBits;
@@ -132,15 +134,17 @@ int batch_prepare(Batch &b, cudaStream_t st)
     if (b.dirty && !b.members.empty()) {  // membership changed: cached autotuner choice, if any
         size_t cells = 0;
         for (const tecto_world *w : b.members) cells += w->N;
-        int th = 0, tr = 0;
-        if (tune_lookup(b.device, cells, b.members.size(), &th, &tr)) {
+        int th = 0, tr = 0, tt = 0;
+        if (tune_lookup(b.device, cells, b.members.size(), &th, &tr, &tt)) {
             b.tuned_hydro = th;
             b.tuned_rb = tr;
+            b.tuned_thermal = tt;
         }
     }
-    int variant = 0, rb = 0;
-    choose_tuning(b, &variant, &rb);
-    if (!b.dirty && variant == b.hydro_variant && rb == b.sort.radix_bits) return TECTO_OK;
+    int variant = 0, rb = 0, tvariant = 0;
+    choose_tuning(b, &variant, &rb, &tvariant);
+    if (!b.dirty && variant == b.hydro_variant && rb == b.sort.radix_bits && tvariant == b.thermal_variant)
+        return TECTO_OK;
     if (b.members.empty()) {
         set_error("batch has no worlds");
         return TECTO_ERR_INVALID;
@@ -150,6 +154,7 @@ int batch_prepare(Batch &b, cudaStream_t st)
     if ((rc = sort_kernel_attributes()) != TECTO_OK) return rc;
     drop_graphs(b);
     b.hydro_variant = variant;
+    b.thermal_variant = tvariant;
     const size_t n = b.members.size();
     std::vector<uint32_t> vbase(n + 1);
     size_t total = 0;

@@ -132,6 +132,8 @@ struct Batch {
     int sort_final = 0;
     size_t total = 0;                        // sum of member cells
     int hydro_variant = 0;                   // tile variant the TK_HYDRO list was built for
+    int thermal_variant = 0;                 // tile variant the TK_THERMAL list was built for
+    int tuned_thermal = 0;
     int tuned_hydro = 0, tuned_rb = 0;       // autotuner's choices (0 = none), used when the
                                              // settings leave hydraulicTile / sortRadixBits at 0
     uint64_t launches = 0;
@@ -276,10 +278,13 @@ int hydro_variant_for(const tecto_settings &s);  // 0 when the settings leave th
 constexpr int kDefaultRadixBits = 8;
 constexpr int kHydroVariantCount = 7;
 constexpr int kDefaultHydroVariant = 4;          // 64 x 32 cells, 1024 threads
+constexpr int kThermalVariantCount = 4;
+constexpr int kDefaultThermalVariant = 4;        // 64 x 16 cells, 512 threads, 2 iterations per launch
+int thermal_variant_for(const tecto_settings &s);  // 0 when the settings leave the choice open
 
 // Autotuner cache (tecto_tune.cu): best hydraulic tile variant and sort digit width for a batch
 // shape class on a device; false when nothing was tuned for that class.
-bool tune_lookup(int device, size_t total_cells, size_t worlds, int *hydro, int *rb);
+bool tune_lookup(int device, size_t total_cells, size_t worlds, int *hydro, int *rb, int *thermal);
 int tune_batch(Batch &b, cudaStream_t st, tecto_tuning *out);  // tune on the members' shapes, apply
 
 // Radix sort core (k_sort.cu).  If worlds != nullptr the first pass generates the keys (the

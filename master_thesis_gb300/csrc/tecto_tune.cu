@@ -1,14 +1,14 @@
-// tecto_tune.cu - the autotuner: picks the hydraulic halo-tile variant and the collision sort's
-// digit width for a batch by timing each candidate on the device.
+// tecto_tune.cu - the autotuner: picks the hydraulic and thermal tile variants and the collision
+// sort's digit width for a batch by timing each candidate on the device.
 //
 // The reference has one fixed launch shape per kernel (src/cuda_compute/plate_tectonic_sim.cu);
 // this engine runs worlds of any size in batches, where the best tile (halo overhead against
-// occupancy) and the best digit width (sort passes against per-tile histogram and look-back
-// cost) depend on the sizes.  Tuning never touches the caller's worlds: it builds scratch
+// occupancy and barrier cost) and the best digit width (sort passes against per-tile histogram
+// and look-back cost) depend on the sizes.  Tuning never touches the caller's worlds: it builds scratch
 // worlds of the same shapes with synthetic content, times the candidates, and frees them.
 // Choices are cached per device and batch shape class (total cells, mean world size, both in
-// half-octave steps); a batch whose settings leave hydraulicTile / sortRadixBits at 0 uses the
-// choice of its class, else of the nearest tuned class on its device.
+// half-octave steps); a batch whose settings leave hydraulicTile / thermalTile / sortRadixBits at
+// 0 uses the choice of its class, else of the nearest tuned class on its device.
 #include <algorithm>
 #include <cmath>
 #include <map>
@@ -26,6 +26,7 @@ namespace {
 struct TuneChoice {
     int hydro;
     int rb;
+    int thermal;
 };
 
 using ClassKey = std::tuple<int, int, int>;  // device, total-cells class, mean-world-cells class
@@ -97,6 +98,7 @@ int tune_shapes(const tecto_settings &settings, const std::vector<int2> &shapes,
     const float dt = settings.step.hydraulicDt;
     if (rc == TECTO_OK) {
         tb.settings.step.hydraulicTile = kDefaultHydroVariant;
+        tb.settings.step.thermalTile = kDefaultThermalVariant;
         tb.settings.step.sortRadixBits = kDefaultRadixBits;
         tb.dirty = true;
         rc = batch_step_graph(tb, 1, st, false);  // plate offsets and a settled state to time on
@@ -117,6 +119,21 @@ int tune_shapes(const tecto_settings &settings, const std::vector<int2> &shapes,
         }
     }
     tb.settings.step.hydraulicTile = best_v;
+    // thermal tile variants: ten iterations each
+    int best_t = kDefaultThermalVariant;
+    float best_tms = INFINITY;
+    for (int v = 1; v <= kThermalVariantCount && rc == TECTO_OK; ++v) {
+        tb.settings.step.thermalTile = v;
+        if ((rc = batch_prepare(tb, st)) != TECTO_OK) break;
+        float ms = 0;
+        rc = time_best(st, 3, &ms, [&]() { return launch_thermal(tb, 10, st); });
+        res.thermal_ms[v - 1] = ms;
+        if (rc == TECTO_OK && ms < best_tms) {
+            best_tms = ms;
+            best_t = v;
+        }
+    }
+    tb.settings.step.thermalTile = best_t;
     // sort digit widths: the key-generating collision sort of the batch
     int best_rb = kDefaultRadixBits;
     float best_sms = INFINITY;
@@ -145,11 +162,12 @@ int tune_shapes(const tecto_settings &settings, const std::vector<int2> &shapes,
     if (rc != TECTO_OK) return rc;
     res.hydraulicTile = best_v;
     res.sortRadixBits = best_rb;
+    res.thermalTile = best_t;
     int dev = 0;
     cudaGetDevice(&dev);
     {
         std::lock_guard<std::mutex> lock(g_tune_mu);
-        g_tune[class_of(dev, total, shapes.size())] = TuneChoice{best_v, best_rb};
+        g_tune[class_of(dev, total, shapes.size())] = TuneChoice{best_v, best_rb, best_t};
     }
     if (out) *out = res;
     return TECTO_OK;
@@ -157,7 +175,7 @@ int tune_shapes(const tecto_settings &settings, const std::vector<int2> &shapes,
 
 }  // namespace
 
-bool tune_lookup(int device, size_t total, size_t worlds, int *hydro, int *rb)
+bool tune_lookup(int device, size_t total, size_t worlds, int *hydro, int *rb, int *thermal)
 {
     std::lock_guard<std::mutex> lock(g_tune_mu);
     const ClassKey k = class_of(device, total, worlds);
@@ -177,6 +195,7 @@ bool tune_lookup(int device, size_t total, size_t worlds, int *hydro, int *rb)
     }
     *hydro = it->second.hydro;
     *rb = it->second.rb;
+    *thermal = it->second.thermal;
     return true;
 }
 
@@ -193,6 +212,7 @@ int tune_batch(Batch &b, cudaStream_t st, tecto_tuning *out)
     if (rc != TECTO_OK) return rc;
     b.tuned_hydro = t.hydraulicTile;
     b.tuned_rb = t.sortRadixBits;
+    b.tuned_thermal = t.thermalTile;
     b.dirty = true;
     if (out) *out = t;
     return TECTO_OK;
@@ -228,22 +248,26 @@ int tecto_batch_autotune(tecto_batch *batch, tecto_stream_t stream, tecto_tuning
     return tune_batch(batch->b, (cudaStream_t)stream, out);
 }
 
-int tecto_autotune_record(int device, size_t total_cells, int worlds, int hydraulicTile, int sortRadixBits)
+int tecto_autotune_record(int device, size_t total_cells, int worlds, int hydraulicTile, int sortRadixBits,
+                          int thermalTile)
 {
     if (device < 0 || total_cells == 0 || worlds < 1 || hydraulicTile < 1 ||
-        hydraulicTile > kHydroVariantCount || !valid_radix_bits(sortRadixBits))
+        hydraulicTile > kHydroVariantCount || !valid_radix_bits(sortRadixBits) || thermalTile < 1 ||
+        thermalTile > kThermalVariantCount)
         return TECTO_ERR_INVALID;
     std::lock_guard<std::mutex> lock(g_tune_mu);
-    g_tune[class_of(device, total_cells, (size_t)worlds)] = TuneChoice{hydraulicTile, sortRadixBits};
+    g_tune[class_of(device, total_cells, (size_t)worlds)] = TuneChoice{hydraulicTile, sortRadixBits, thermalTile};
     return TECTO_OK;
 }
 
-int tecto_autotune_lookup(int device, size_t total_cells, int worlds, int *hydraulicTile, int *sortRadixBits)
+int tecto_autotune_lookup(int device, size_t total_cells, int worlds, int *hydraulicTile, int *sortRadixBits,
+                          int *thermalTile)
 {
-    if (!hydraulicTile || !sortRadixBits || worlds < 1) return TECTO_ERR_INVALID;
-    if (!tune_lookup(device, total_cells, (size_t)worlds, hydraulicTile, sortRadixBits)) {
+    if (!hydraulicTile || !sortRadixBits || !thermalTile || worlds < 1) return TECTO_ERR_INVALID;
+    if (!tune_lookup(device, total_cells, (size_t)worlds, hydraulicTile, sortRadixBits, thermalTile)) {
         *hydraulicTile = 0;
         *sortRadixBits = 0;
+        *thermalTile = 0;
         return TECTO_ERR_NOT_FOUND;
     }
     return TECTO_OK;

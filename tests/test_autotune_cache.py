@@ -19,29 +19,29 @@ def test_empty_cache_finds_nothing():
 
 
 def test_record_and_exact_lookup():
-    T.autotune_record(0, 48_000_000, 256, 3, 9)
-    assert T.autotune_lookup(0, 48_000_000, 256) == (3, 9)
+    T.autotune_record(0, 48_000_000, 256, 3, 9, 2)
+    assert T.autotune_lookup(0, 48_000_000, 256) == (3, 9, 2)
     # same half-octave classes
-    assert T.autotune_lookup(0, 49_000_000, 256) == (3, 9)
+    assert T.autotune_lookup(0, 49_000_000, 256) == (3, 9, 2)
 
 
 def test_nearest_class_on_the_same_device():
-    T.autotune_record(0, 1 << 16, 1, 1, 8)      # small single world
-    T.autotune_record(0, 1 << 26, 256, 4, 11)   # large batch
-    assert T.autotune_lookup(0, 1 << 17, 1) == (1, 8)
-    assert T.autotune_lookup(0, 1 << 25, 200) == (4, 11)
+    T.autotune_record(0, 1 << 16, 1, 1, 8, 1)      # small single world
+    T.autotune_record(0, 1 << 26, 256, 4, 11, 4)   # large batch
+    assert T.autotune_lookup(0, 1 << 17, 1) == (1, 8, 1)
+    assert T.autotune_lookup(0, 1 << 25, 200) == (4, 11, 4)
     assert T.autotune_lookup(1, 1 << 26, 256) is None  # other device: nothing tuned
 
 
 def test_later_record_replaces():
-    T.autotune_record(0, 1 << 22, 1, 2, 8)
-    T.autotune_record(0, 1 << 22, 1, 5, 10)
-    assert T.autotune_lookup(0, 1 << 22, 1) == (5, 10)
+    T.autotune_record(0, 1 << 22, 1, 2, 8, 1)
+    T.autotune_record(0, 1 << 22, 1, 5, 10, 3)
+    assert T.autotune_lookup(0, 1 << 22, 1) == (5, 10, 3)
 
 
-@pytest.mark.parametrize("args", [(0, 1 << 20, 1, 0, 8), (0, 1 << 20, 1, 8, 8), (0, 1 << 20, 1, 4, 7),
-                                  (0, 1 << 20, 1, 4, 12), (0, 0, 1, 4, 8), (0, 1 << 20, 0, 4, 8),
-                                  (-1, 1 << 20, 1, 4, 8)])
+@pytest.mark.parametrize("args", [(0, 1 << 20, 1, 0, 8, 1), (0, 1 << 20, 1, 8, 8, 1), (0, 1 << 20, 1, 4, 7, 1),
+                                  (0, 1 << 20, 1, 4, 12, 1), (0, 0, 1, 4, 8, 1), (0, 1 << 20, 0, 4, 8, 1),
+                                  (-1, 1 << 20, 1, 4, 8, 1), (0, 1 << 20, 1, 4, 8, 0), (0, 1 << 20, 1, 4, 8, 5)])
 def test_invalid_records_rejected(args):
     with pytest.raises(T.TectoError):
         T.autotune_record(*args)

@@ -138,6 +138,22 @@ def test_hydraulic_tile_variants_match_oracle(tile, W, H, dt):
     w.check()
 
 
+@pytest.mark.parametrize("tile", [1, 2, 3, 4])
+@pytest.mark.parametrize("W,H,iters", [(100, 60, 7), (33, 17, 5), (300, 200, 10), (128, 96, 3)])
+def test_thermal_tile_variants_match_oracle(tile, W, H, iters):
+    """Every thermal tile shape and per-launch iteration split gives the oracle's result."""
+    st, w = make_world("baseline", W, H)
+    st.step.thermalTile = tile
+    w.set_settings(st)
+    rng = np.random.default_rng(W + H + tile)
+    h = (w.download(T.FIELD_HEIGHT) + rng.normal(0, 0.05, (H, W))).astype(np.float32)
+    w.upload(T.FIELD_HEIGHT, h)
+    w.thermal(iters)
+    want = O.thermal(h, iters, st)
+    np.testing.assert_array_equal(w.download(T.FIELD_HEIGHT), want)
+    w.check()
+
+
 @pytest.mark.parametrize("W,H,steps", [(64, 64, 12), (100, 60, 12), (256, 256, 6)])
 def test_graph_steps_match_oracle(torch_stream, W, H, steps):
     st, w = make_world("baseline", W, H)

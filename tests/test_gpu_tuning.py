@@ -109,14 +109,16 @@ def test_world_autotune_keeps_results(stream):
     w.check(stream)
     for f in FIELDS:
         np.testing.assert_array_equal(w.download(f), plain.download(f), err_msg=f"field {f}")
-    assert T.autotune_lookup(0, W * H, 1) == (t.hydraulicTile, t.sortRadixBits)
+    assert T.autotune_lookup(0, W * H, 1) == (t.hydraulicTile, t.sortRadixBits, t.thermalTile)
+    assert 1 <= t.thermalTile <= 4 and t.thermal_ms[t.thermalTile - 1] == min(t.thermal_ms)
 
 
 def test_shape_autotune_and_batch_autotune(stream):
     T.autotune_clear()
     shapes = [(256, 256), (512, 256), (128, 128), (1024, 512)]
     t = T.autotune(settings(), shapes, stream)
-    assert T.autotune_lookup(0, sum(a * b for a, b in shapes), len(shapes)) == (t.hydraulicTile, t.sortRadixBits)
+    assert T.autotune_lookup(0, sum(a * b for a, b in shapes), len(shapes)) == (t.hydraulicTile, t.sortRadixBits,
+                                                                                 t.thermalTile)
     b = T.Batch()
     ws = []
     for i, (W, H) in enumerate(shapes):
