@@ -146,16 +146,21 @@ def mixed_worlds(n=N_WORLDS, seed=SHAPE_SEED):
 
 
 def serve_trace(n, mean_service_s, load, seed=7, saturated=False):
-    """Poisson arrivals at `load` x the plain path's capacity (1 / mean service time)."""
+    """Poisson arrivals at `load` x the plain path's capacity (1 / mean service time).  Sizes are
+    stratified (70 % 256^2, 25 % 1024^2, 5 % 4096^2 of the n requests, in random order) so that a
+    short trace carries the size mix it is meant to."""
     import master_thesis_gb300 as T
 
     rng = np.random.default_rng(seed)
     lam = load / mean_service_s
+    n_big = max(1, round(0.05 * n))
+    n_mid = round(0.25 * n)
+    sides = np.array([4096] * n_big + [1024] * n_mid + [256] * (n - n_big - n_mid))
+    rng.shuffle(sides)
     t = 0.0
     reqs = []
     for i in range(n):
-        u = rng.uniform()
-        side = 256 if u < 0.70 else (1024 if u < 0.95 else 4096)
+        side = int(sides[i])
         steps = int(rng.integers(50, 501))
         plates = int(rng.integers(8, 49))
         t += rng.exponential(1.0 / lam)
@@ -432,7 +437,14 @@ def engine_extras(args, T, torch, stream, s, specs, total, batched_value):
     peak, _ = measured_peak_hbm()
     out = {}
 
-    # the same worlds, one at a time through the plain path
+    # the same worlds, one at a time through the plain path, each with the autotuner's choice for
+    # a single world of its size class (one representative shape tuned per class)
+    classes = {}
+    for W, H, *_ in specs:
+        key = (round(2 * math.log2(W * H)),)
+        classes.setdefault(key, (W, H))
+    for W, H in classes.values():
+        T.autotune(s, [(W, H)], stream)
     k = 4
     plain_ms = 0.0
     for W, H, P, gs, wsd in specs:
@@ -448,7 +460,8 @@ def engine_extras(args, T, torch, stream, s, specs, total, batched_value):
     plain_value = total * k / (plain_ms / 1e3)
     out["plain"] = {"value": plain_value, "unit": "cell-updates/s",
                     "workload": f"the same {N_WORLDS} worlds stepped one at a time on the plain path "
-                                f"({k} steps each, graph replay)",
+                                f"({k} steps each, graph replay, autotuned per size class: "
+                                f"{len(classes)} classes)",
                     "batched_vs_plain": batched_value / plain_value}
 
     # plain one-world references
@@ -553,7 +566,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
-    ap.add_argument("--serve-requests", type=int, default=40)
+    ap.add_argument("--serve-requests", type=int, default=64)
     ap.add_argument("--quick", action="store_true", help="headline only (no plain/served/large-world lines)")
     ap.add_argument("--case", choices=["erosion2048", "plain2048", "batch"], help="a small fixed workload for profilers")
     args = ap.parse_args()
