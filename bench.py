@@ -20,7 +20,7 @@ and sort digit width picked by the autotuner.  Beside it:
   plain_2048   one 2048^2 world, 32 plates (plain path; its k_hydro roofline);
   plain_8192   one 8192^2 world, 64 plates, velocities in [-2, 2], 8-connected CCL every step.
 `e2e` repeats the headline through the C ABI with host buffers: every step uploads each world's
-state from pinned host memory, steps the batch, and downloads heights and plate ids.
+state from pinned host memory, steps the batch, downloads heights and plate ids, and waits for them.
 Reference arm: the reference path's CPU implementation (the oracle's C restatement, all host
 threads) on a bounded sample of the same mixed-size workload.  With N > 1 (torchrun) every rank
 runs its own batch (replicas; worlds never exchange data).
@@ -362,14 +362,17 @@ def run_engine(args, ws, rank, local):
     outs = [{f: torch.empty_like(h[f]).pin_memory() for f in down_fields} for h in hosts]
 
     def e2e_step():
+        # stream-ordered copies from / to pinned host buffers, one wait per step
         for w, hs in zip(worlds, hosts):
             for f, t in hs.items():
-                T.check(L.tecto_world_upload(w.ptr, f, t.data_ptr(), t.numel() * t.element_size(), sp), "upload")
+                T.check(L.tecto_world_upload_async(w.ptr, f, t.data_ptr(), t.numel() * t.element_size(), sp),
+                        "upload")
         batch.step(1, stream)
         for w, os_ in zip(worlds, outs):
             for f, t in os_.items():
-                T.check(L.tecto_world_download(w.ptr, f, t.data_ptr(), t.numel() * t.element_size(), sp),
+                T.check(L.tecto_world_download_async(w.ptr, f, t.data_ptr(), t.numel() * t.element_size(), sp),
                         "download")
+        stream.synchronize()
 
     e2e_step()
     stream.synchronize()

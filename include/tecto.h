@@ -228,6 +228,11 @@ int tecto_world_upload(tecto_world *world, int field, const void *host, size_t b
                        tecto_stream_t stream);
 int tecto_world_download(tecto_world *world, int field, void *host, size_t bytes,
                          tecto_stream_t stream);
+/* The same copies ordered on the stream without waiting for them: the host buffer (pinned for
+ * asynchrony) must stay valid, and a download's unread, until the stream reaches the copy. */
+int tecto_world_upload_async(tecto_world *world, int field, const void *host, size_t bytes,
+                             tecto_stream_t stream);
+int tecto_world_download_async(tecto_world *world, int field, void *host, size_t bytes, tecto_stream_t stream);
 /* Borrow the device pointer of a field (valid until the next call that steps the world). */
 int tecto_world_field(tecto_world *world, int field, void **device_ptr, size_t *bytes);
 

@@ -217,6 +217,8 @@ def _declare(L: C.CDLL) -> None:
         "tecto_world_init_synthetic": ([P, C.c_int, C.c_float, C.c_uint64, P], C.c_int),
         "tecto_world_upload": ([P, C.c_int, P, C.c_size_t, P], C.c_int),
         "tecto_world_download": ([P, C.c_int, P, C.c_size_t, P], C.c_int),
+        "tecto_world_upload_async": ([P, C.c_int, P, C.c_size_t, P], C.c_int),
+        "tecto_world_download_async": ([P, C.c_int, P, C.c_size_t, P], C.c_int),
         "tecto_world_field": ([P, C.c_int, C.POINTER(P), C.POINTER(C.c_size_t)], C.c_int),
         "tecto_world_set_plates": ([P, P, C.c_int, P], C.c_int),
         "tecto_world_get_plates": ([P, P, C.c_int, P], C.c_int),

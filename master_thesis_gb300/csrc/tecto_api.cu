@@ -548,6 +548,37 @@ int tecto_world_download(tecto_world *w, int field, void *host, size_t bytes, te
     return TECTO_OK;
 }
 
+// Stream-ordered copies with no synchronisation: the caller keeps the host buffer alive (and, for
+// a download, unread) until the stream has reached this point.
+static int copy_field_async(tecto_world *w, int field, void *host, size_t bytes, cudaStream_t st, bool up,
+                            const char *who)
+{
+    int rc = check_world(w);
+    if (rc != TECTO_OK) return rc;
+    void *p;
+    size_t n;
+    field_info(w, field, &p, &n);
+    if (!p || !host || bytes != n) {
+        set_error(std::string(who) + ": unknown field or size mismatch");
+        return TECTO_ERR_INVALID;
+    }
+    if ((rc = bind_device(w)) != TECTO_OK) return rc;
+    if (up) TECTO_CUDA(cudaMemcpyAsync(p, host, n, cudaMemcpyHostToDevice, st));
+    else TECTO_CUDA(cudaMemcpyAsync(host, p, n, cudaMemcpyDeviceToHost, st));
+    return TECTO_OK;
+}
+
+int tecto_world_upload_async(tecto_world *w, int field, const void *host, size_t bytes, tecto_stream_t stream)
+{
+    return copy_field_async(w, field, const_cast<void *>(host), bytes, (cudaStream_t)stream, true,
+                            "tecto_world_upload_async");
+}
+
+int tecto_world_download_async(tecto_world *w, int field, void *host, size_t bytes, tecto_stream_t stream)
+{
+    return copy_field_async(w, field, host, bytes, (cudaStream_t)stream, false, "tecto_world_download_async");
+}
+
 int tecto_world_set_plates(tecto_world *w, const tecto_plate *plates, int count, tecto_stream_t stream)
 {
     int rc = check_world(w);

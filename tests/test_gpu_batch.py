@@ -132,3 +132,27 @@ def test_server_continuous_batching_matches_one_at_a_time(stream):
     stream.synchronize()
     assert np.float32(w.download(T.FIELD_HEIGHT).astype(np.float64).sum()) == res_c[5].height_checksum
     sv.close()
+
+
+def test_async_field_copies_round_trip(stream):
+    """tecto_world_upload_async / download_async are stream-ordered: upload, step, download and
+    one wait give the same fields as the synchronous calls."""
+    torch = pytest.importorskip("torch")
+    s = settings()
+    a, b = make(SPECS[4], s), make(SPECS[4], s)
+    W, H = SPECS[4][0], SPECS[4][1]
+    rng = np.random.default_rng(2)
+    water = torch.from_numpy(np.abs(rng.normal(0, 0.1, (H, W))).astype(np.float32)).pin_memory()
+    out = torch.empty((H, W), dtype=torch.float32).pin_memory()
+    L = T.lib()
+    sp = stream.cuda_stream
+    T.check(L.tecto_world_upload_async(a.ptr, T.FIELD_WATER, water.data_ptr(), W * H * 4, sp), "upload_async")
+    a.step(2, stream)
+    T.check(L.tecto_world_download_async(a.ptr, T.FIELD_WATER, out.data_ptr(), W * H * 4, sp), "download_async")
+    stream.synchronize()
+    b.upload(T.FIELD_WATER, water.numpy())
+    b.step(2, stream)
+    stream.synchronize()
+    np.testing.assert_array_equal(out.numpy(), b.download(T.FIELD_WATER))
+    with pytest.raises(T.TectoError):
+        T.check(L.tecto_world_upload_async(a.ptr, T.FIELD_WATER, water.data_ptr(), 12, sp), "upload_async")
