@@ -405,6 +405,16 @@ int tecto_server_run_trace(tecto_server *server, const tecto_request *requests, 
 int tecto_server_run_trace_sequential(tecto_server *server, const tecto_request *requests, int n,
                                       tecto_stream_t stream, tecto_request_result *results,
                                       tecto_server_stats *stats);
+/* Headless output of served results: each request that finishes writes, into `directory`,
+ * request_<i>_height.png (TECTO_SERVER_OUT_HEIGHT_PNG: the 16-bit export over [height_min,
+ * height_max]), request_<i>_plates.png (TECTO_SERVER_OUT_PLATES_PNG) and request_<i>.snap
+ * (TECTO_SERVER_OUT_SNAPSHOT), i its index in the trace, before its world is released.  A failed
+ * write sets that request's status.  what = 0 turns output off.  Dry runs write nothing. */
+#define TECTO_SERVER_OUT_HEIGHT_PNG 1
+#define TECTO_SERVER_OUT_PLATES_PNG 2
+#define TECTO_SERVER_OUT_SNAPSHOT 4
+int tecto_server_set_output(tecto_server *server, const char *directory, int what, float height_min,
+                            float height_max);
 /* Dry-run cost model: seconds one tick takes per million active cells (default 2e-4). */
 int tecto_server_set_dry_cost(tecto_server *server, double seconds_per_mcell_step);
 
@@ -412,6 +422,42 @@ int tecto_server_set_dry_cost(tecto_server *server, double seconds_per_mcell_ste
  * (the on-device world init the server uses). */
 int tecto_world_init_synthetic_device(tecto_world *world, int numPlates, float velRange,
                                       uint64_t genSeed, tecto_stream_t stream);
+
+/* ---- output and checkpoints ------------------------------------------------------------ */
+
+/* PNG encoding of a host image (kind: TECTO_PNG_GRAY16 = uint16 per pixel in host order,
+ * TECTO_PNG_RGB8 = 3 bytes per pixel, TECTO_PNG_GRAY8 = 1 byte), rows top to bottom.  The encoder
+ * writes stored deflate blocks (no compression).  out == NULL: only *written (the file size) is
+ * set. */
+#define TECTO_PNG_GRAY16 0
+#define TECTO_PNG_RGB8 1
+#define TECTO_PNG_GRAY8 2
+int tecto_png_encode(const void *pixels, int width, int height, int kind, void *out, size_t capacity,
+                     size_t *written);
+
+/* The reference's two image exports (src/cuda_compute/texture_save.cu), written as a PNG file:
+ *  TECTO_EXPORT_HEIGHT_GRAY16  saveFloatCudaTextureToDiskAsGray16: (uint16)(clamp((h - min) /
+ *                              (max - min), 0, 1) * 65535), converted on the device; the reference
+ *                              passes minUpliftClamp / maxUpliftClamp (plate_tectonic_sim.cu:635);
+ *                              the file carries the reference's sRGB chunk (perceptual intent);
+ *  TECTO_EXPORT_PLATES_RGB     saveGrayscale8BitCudaTextureToDiskAsRgb: one HSV colour per plate
+ *                              id, id 255 the background (230, 235, 240); min/max unused.
+ * Synchronous on `stream`. */
+/* The colour of each plate id as the RGB export uses it (rgb768[3 * id + c]). */
+int tecto_plate_palette(uint8_t *rgb768);
+#define TECTO_EXPORT_HEIGHT_GRAY16 0
+#define TECTO_EXPORT_PLATES_RGB 1
+int tecto_world_export_png(tecto_world *world, int kind, const char *path, float min_value, float max_value,
+                           tecto_stream_t stream);
+
+/* Checkpoint / resume: the complete state a step reads (heights, water, sediment, flux, plate ids,
+ * CCL labels, pair type bitmap, divergence bitmap, plate records, settings, seed, iteration) as one
+ * file.  A world of the same size loaded from it steps bit-identically to the saved world.  The
+ * reference has no counterpart (it restarts from config.json and its seed). */
+int tecto_world_save_snapshot(tecto_world *world, const char *path, tecto_stream_t stream);
+int tecto_world_load_snapshot(tecto_world *world, const char *path, tecto_stream_t stream);
+/* Size and settings stored in a snapshot file, to create the world that loads it. */
+int tecto_snapshot_info(const char *path, int *width, int *height, tecto_settings *settings);
 
 /* ---- status -------------------------------------------------------------------------- */
 

@@ -33,6 +33,9 @@ NUM_DIV_WORDS = 1013
 
 UPLIFT_GAUSSIAN, UPLIFT_NONE, UPLIFT_REFERENCE = 0, 1, 2
 CCL_4, CCL_8, CCL_REF8 = 4, 8, 9
+PNG_GRAY16, PNG_RGB8, PNG_GRAY8 = 0, 1, 2
+EXPORT_HEIGHT_GRAY16, EXPORT_PLATES_RGB = 0, 1
+SERVER_OUT_HEIGHT_PNG, SERVER_OUT_PLATES_PNG, SERVER_OUT_SNAPSHOT = 1, 2, 4
 
 (FIELD_HEIGHT, FIELD_WATER, FIELD_SEDIMENT, FIELD_FLUX, FIELD_PLATE_ID, FIELD_LABELS,
  FIELD_COLLISION, FIELD_TYPE_BITMAP, FIELD_DIV_BITMAP, FIELD_SORT_KEYS, FIELD_SORT_VALS,
@@ -262,7 +265,14 @@ def _declare(L: C.CDLL) -> None:
         "tecto_server_run_trace_sequential": ([P, C.POINTER(Request), C.c_int, P, C.POINTER(RequestResult),
                                                C.POINTER(ServerStats)], C.c_int),
         "tecto_server_set_dry_cost": ([P, C.c_double], C.c_int),
+        "tecto_server_set_output": ([P, C.c_char_p, C.c_int, C.c_float, C.c_float], C.c_int),
         "tecto_selftest_div": ([P, P, P, C.c_size_t, P], C.c_int),
+        "tecto_png_encode": ([P, C.c_int, C.c_int, C.c_int, P, C.c_size_t, C.POINTER(C.c_size_t)], C.c_int),
+        "tecto_plate_palette": ([P], C.c_int),
+        "tecto_world_export_png": ([P, C.c_int, C.c_char_p, C.c_float, C.c_float, P], C.c_int),
+        "tecto_world_save_snapshot": ([P, C.c_char_p, P], C.c_int),
+        "tecto_world_load_snapshot": ([P, C.c_char_p, P], C.c_int),
+        "tecto_snapshot_info": ([C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(Settings)], C.c_int),
         "tecto_last_error_string": ([], C.c_char_p),
         "tecto_version": ([], C.c_char_p),
     }
@@ -443,6 +453,57 @@ class World:
     def check(self, stream=None):
         check(lib().tecto_world_check(self.ptr, _stream(stream)), "tecto_world_check")
 
+    def export_png(self, kind: int, path, min_value: float = 0.0, max_value: float = 1.0, stream=None) -> None:
+        """Write the height map (EXPORT_HEIGHT_GRAY16, normalised over [min_value, max_value]) or
+        the plate ids (EXPORT_PLATES_RGB) as a PNG file."""
+        check(lib().tecto_world_export_png(self.ptr, kind, os.fsencode(path), min_value, max_value,
+                                           _stream(stream)), "tecto_world_export_png")
+
+    def save_snapshot(self, path, stream=None) -> None:
+        check(lib().tecto_world_save_snapshot(self.ptr, os.fsencode(path), _stream(stream)),
+              "tecto_world_save_snapshot")
+
+    def load_snapshot(self, path, stream=None) -> None:
+        check(lib().tecto_world_load_snapshot(self.ptr, os.fsencode(path), _stream(stream)),
+              "tecto_world_load_snapshot")
+
+    @classmethod
+    def from_snapshot(cls, path, stream=None) -> "World":
+        """A new world of the snapshot's size and settings, holding its state."""
+        W, H, s = snapshot_info(path)
+        w = cls(s, W, H)
+        w.load_snapshot(path, stream)
+        return w
+
+
+def snapshot_info(path) -> tuple[int, int, Settings]:
+    W, H, s = C.c_int(0), C.c_int(0), Settings()
+    check(lib().tecto_snapshot_info(os.fsencode(path), C.byref(W), C.byref(H), C.byref(s)),
+          "tecto_snapshot_info")
+    return W.value, H.value, s
+
+
+def plate_palette() -> np.ndarray:
+    """The RGB colour of each plate id in the plate export: uint8[256, 3]."""
+    out = np.empty((256, 3), np.uint8)
+    check(lib().tecto_plate_palette(out.ctypes.data), "tecto_plate_palette")
+    return out
+
+
+def png_encode(pixels: np.ndarray, kind: int) -> bytes:
+    """PNG file bytes of a host image: PNG_GRAY16 (uint16 [H,W]), PNG_RGB8 (uint8 [H,W,3]) or
+    PNG_GRAY8 (uint8 [H,W])."""
+    dt, nd = {PNG_GRAY16: (np.uint16, 2), PNG_RGB8: (np.uint8, 3), PNG_GRAY8: (np.uint8, 2)}[kind]
+    a = np.ascontiguousarray(pixels, dtype=dt)
+    if a.ndim != nd or (kind == PNG_RGB8 and a.shape[2] != 3):
+        raise ValueError(f"png_encode: bad image shape {a.shape} for kind {kind}")
+    n = C.c_size_t(0)
+    H, W = a.shape[0], a.shape[1]
+    check(lib().tecto_png_encode(a.ctypes.data, W, H, kind, None, 0, C.byref(n)), "tecto_png_encode")
+    out = C.create_string_buffer(n.value)
+    check(lib().tecto_png_encode(a.ctypes.data, W, H, kind, out, n.value, C.byref(n)), "tecto_png_encode")
+    return out.raw[: n.value]
+
 
 def _world_init_device(self, plates: int, vel_range: float, gen_seed: int, stream=None) -> None:
     check(lib().tecto_world_init_synthetic_device(self.ptr, plates, vel_range, gen_seed, _stream(stream)),
@@ -551,6 +612,11 @@ class Server:
         check(lib().tecto_server_create(C.byref(settings), budget_bytes, max_worlds,
                                         SERVER_DRY_RUN if dry_run else 0, C.byref(p)), "tecto_server_create")
         self.ptr = p
+
+    def set_output(self, directory, what: int, height_min: float = 0.0, height_max: float = 1.0) -> None:
+        """Write finished requests' exports and snapshots (SERVER_OUT_* bits) into `directory`."""
+        d = os.fsencode(directory) if directory is not None else None
+        check(lib().tecto_server_set_output(self.ptr, d, what, height_min, height_max), "tecto_server_set_output")
 
     def set_dry_cost(self, seconds_per_mcell_step: float) -> None:
         check(lib().tecto_server_set_dry_cost(self.ptr, seconds_per_mcell_step), "tecto_server_set_dry_cost")

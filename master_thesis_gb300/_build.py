@@ -29,6 +29,7 @@ SOURCES = [
     "k_resolve.cu",
     "k_erosion.cu",
     "k_ccl.cu",
+    "tecto_export.cu",
     "settings.cpp",
 ]
 

@@ -11,6 +11,7 @@
 #include <cmath>
 #include <deque>
 #include <new>
+#include <string>
 #include <thread>
 #include <vector>
 
@@ -30,6 +31,9 @@ struct tecto_server {
     bool dry = false;
     double dry_cost = 2e-4;  // seconds per tick per million active cells
     tecto_batch *batch = nullptr;
+    std::string out_dir;     // where finished requests are written (tecto_server_set_output)
+    int out_what = 0;        // TECTO_SERVER_OUT_* bits
+    float out_lo = 0.0f, out_hi = 1.0f;  // height range of the 16-bit export
 };
 
 namespace {
@@ -103,6 +107,33 @@ float checksum(tecto_world *w, cudaStream_t st)
     return (float)s;
 }
 
+// The outputs a finished request asked for, named by its index in the trace.
+int write_outputs(const tecto_server *sv, tecto_world *w, int idx, cudaStream_t st)
+{
+    const std::string base = sv->out_dir + "/request_" + std::to_string(idx);
+    int rc = TECTO_OK;
+    if (sv->out_what & TECTO_SERVER_OUT_HEIGHT_PNG)
+        rc = tecto_world_export_png(w, TECTO_EXPORT_HEIGHT_GRAY16, (base + "_height.png").c_str(), sv->out_lo,
+                                    sv->out_hi, (tecto_stream_t)st);
+    if (rc == TECTO_OK && (sv->out_what & TECTO_SERVER_OUT_PLATES_PNG))
+        rc = tecto_world_export_png(w, TECTO_EXPORT_PLATES_RGB, (base + "_plates.png").c_str(), 0.0f, 0.0f,
+                                    (tecto_stream_t)st);
+    if (rc == TECTO_OK && (sv->out_what & TECTO_SERVER_OUT_SNAPSHOT))
+        rc = tecto_world_save_snapshot(w, (base + ".snap").c_str(), (tecto_stream_t)st);
+    return rc;
+}
+
+// A finished request's result: its checksum and the outputs it asked for (a failed write marks the
+// request failed; serving goes on).
+void finish_world(const tecto_server *sv, tecto_world *w, int idx, cudaStream_t st, tecto_request_result &res)
+{
+    res.height_checksum = checksum(w, st);
+    if (sv->out_what) {
+        const int rc = write_outputs(sv, w, idx, st);
+        if (rc != TECTO_OK) res.status = rc;
+    }
+}
+
 bool valid_request(const tecto_request &r)
 {
     return r.width >= 1 && r.height >= 1 && r.plates >= 1 && r.plates <= kPlates && r.steps >= 0 &&
@@ -132,6 +163,21 @@ int tecto_server_destroy(tecto_server *sv)
     if (!sv) return TECTO_OK;
     if (sv->batch) tecto_batch_destroy(sv->batch);
     delete sv;
+    return TECTO_OK;
+}
+
+int tecto_server_set_output(tecto_server *server, const char *directory, int what, float height_min,
+                            float height_max)
+{
+    if (!server || what < 0 || what > 7 || (what && !directory) ||
+        ((what & TECTO_SERVER_OUT_HEIGHT_PNG) && !(height_max > height_min))) {
+        set_error("tecto_server_set_output: invalid argument");
+        return TECTO_ERR_INVALID;
+    }
+    server->out_dir = what ? directory : "";
+    server->out_what = what;
+    server->out_lo = height_min;
+    server->out_hi = height_max;
     return TECTO_OK;
 }
 
@@ -207,7 +253,7 @@ int tecto_server_run_trace(tecto_server *sv, const tecto_request *req, int n, te
             if (live[k].steps_left > 0) { ++k; continue; }
             const int i = live[k].idx;
             if (!sv->dry) {
-                res[i].height_checksum = checksum(live[k].world, st);
+                finish_world(sv, live[k].world, i, st, res[i]);
                 tecto_batch_remove(sv->batch, live[k].world);
                 tecto_world_destroy(live[k].world);
             }
@@ -242,7 +288,7 @@ int tecto_server_run_trace(tecto_server *sv, const tecto_request *req, int n, te
             if (--live[k].steps_left > 0) { ++k; continue; }
             const int i = live[k].idx;
             if (!sv->dry) {
-                res[i].height_checksum = checksum(live[k].world, st);
+                finish_world(sv, live[k].world, i, st, res[i]);
                 tecto_batch_remove(sv->batch, live[k].world);
                 tecto_world_destroy(live[k].world);
             }
@@ -305,7 +351,7 @@ int tecto_server_run_trace_sequential(tecto_server *sv, const tecto_request *req
                 tecto_world_destroy(w);
                 return rc;
             }
-            res[i].height_checksum = checksum(w, st);
+            finish_world(sv, w, i, st, res[i]);
             tecto_world_destroy(w);
         }
         ticks += r.steps;

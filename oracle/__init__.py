@@ -23,7 +23,7 @@ _r = None
 def build(ref: bool = False) -> None:
     """make the oracle and the reference-GPU timing harness (and, with ref=True, the
     reference-on-CPU library and the reference's device code for the GPU)."""
-    targets = ["all", "harness"] + (["ref", "refgpu"] if ref else [])
+    targets = ["all", "harness"] + (["ref", "refgpu", "refexport"] if ref else [])
     subprocess.run(["make", "-s", "-C", str(HERE), *targets], check=True)
 
 
@@ -54,6 +54,42 @@ def ref_gpu_time(W, H, h, ids, plates, settings, steps=5, warmup=2):
     return ms.value
 
 
+REF_EXPORT_CUBIN = HERE / "_ref" / "ref_export.cubin"
+
+
+def _ref_export_lib():
+    if not REF_EXPORT_CUBIN.exists():
+        raise RuntimeError("the reference's export kernels were not built (oracle/_ref/ref_export.cubin is absent)")
+    L = C.CDLL(str(REF_GPU_LIB))
+    L.refgpu_error.restype = C.c_char_p
+    L.refgpu_export_load.argtypes = [C.c_char_p]
+    L.refgpu_gray16.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float, C.c_void_p]
+    L.refgpu_ids_rgb.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+    if L.refgpu_export_load(str(REF_EXPORT_CUBIN).encode()) != 0:
+        raise RuntimeError(L.refgpu_error().decode())
+    return L
+
+
+def ref_gpu_gray16(h, minv, maxv):
+    """The reference's convertFloatToGray16Kernel run on this GPU: uint16[H, W]."""
+    L = _ref_export_lib()
+    h = np.ascontiguousarray(h, np.float32)
+    out = np.empty(h.shape, np.uint16)
+    if L.refgpu_gray16(h.ctypes.data, h.shape[1], h.shape[0], minv, maxv, out.ctypes.data) != 0:
+        raise RuntimeError(L.refgpu_error().decode())
+    return out
+
+
+def ref_gpu_ids_rgb(ids):
+    """The reference's convertGrayscaleToRgbKernel run on this GPU: uint8[H, W, 3]."""
+    L = _ref_export_lib()
+    ids = np.ascontiguousarray(ids, np.uint8)
+    out = np.empty(ids.shape + (3,), np.uint8)
+    if L.refgpu_ids_rgb(ids.ctypes.data, ids.shape[1], ids.shape[0], out.ctypes.data) != 0:
+        raise RuntimeError(L.refgpu_error().decode())
+    return out
+
+
 def _P(a):
     return a.ctypes.data if a is not None else None
 
@@ -76,6 +112,8 @@ def lib() -> C.CDLL:
         L.or_expf.restype = C.c_float
         L.or_log10f.argtypes = [C.c_float]
         L.or_log10f.restype = C.c_float
+        L.or_gray16.argtypes = [C.c_size_t, V, C.c_float, C.c_float, V]
+        L.or_plate_palette.argtypes = [V]
         L.or_thermal.argtypes = [C.c_int, C.c_int, V, C.c_int, V]
         L.or_hydraulic.argtypes = [C.c_int, C.c_int, V, V, V, V, C.c_int, C.c_float, C.c_uint32, V]
         L.or_accretion.argtypes = [C.c_int, C.c_int, V, V, V, V]
@@ -123,6 +161,8 @@ def ref() -> C.CDLL:
         L.ref_hydraulic.restype = C.c_int
         L.ref_accretion.argtypes = [C.c_int, C.c_int, V, V, V]
         L.ref_ccl.argtypes = [C.c_int, C.c_int, V, V]
+        L.ref_gray16.argtypes = [C.c_int, C.c_int, V, C.c_float, C.c_float, V]
+        L.ref_ids_rgb.argtypes = [C.c_int, C.c_int, V, V]
         _r = L
     return _r
 
@@ -197,6 +237,21 @@ def expf(x: float) -> float:
 
 def log10f(x: float) -> float:
     return lib().or_log10f(x)
+
+
+def gray16(h, minv, maxv):
+    """convertFloatToGray16Kernel (texture_save.cu:80-96) on the CPU."""
+    h = np.ascontiguousarray(h, np.float32)
+    out = np.empty(h.shape, np.uint16)
+    lib().or_gray16(h.size, h.ctypes.data, minv, maxv, out.ctypes.data)
+    return out
+
+
+def plate_palette():
+    """convertGrayscaleToRgbKernel's colour of each plate id (texture_save.cu:16-70): uint8[256, 3]."""
+    out = np.empty((256, 3), np.uint8)
+    lib().or_plate_palette(out.ctypes.data)
+    return out
 
 
 def thermal(h, iters, settings):

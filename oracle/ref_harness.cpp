@@ -19,6 +19,14 @@
 #include "plate_tectonic_sim.h"
 #include "../include/tecto.h"
 
+/* the two conversion kernels of the reference's image export (texture_save.cu:10-97, compiled by
+ * oracle/Makefile from the lines where they lie) */
+namespace texture_save_detail {
+void convertGrayscaleToRgbKernel(const CudaTexture<uint8_t> *r_texture, uint8_t *w_texture);
+void convertFloatToGray16Kernel(const CudaTexture<float> *r_texture, uint16_t *w_texture, float minVal,
+                                float maxVal);
+}  // namespace texture_save_detail
+
 thread_local uint3 threadIdx;
 thread_local uint3 blockIdx;
 thread_local dim3 blockDim;
@@ -265,6 +273,25 @@ void ref_ccl(int W, int H, const uint8_t *id, uint32_t *labels)
     launch(blocks_for(N), TPB, [&] { analyzeClamped(&tL); });
     launch(blocks_for(N), TPB, [&] { reduce(&tId, &tL); });
     launch(blocks_for(N), TPB, [&] { analyzeUnclamped(&tL); });
+}
+
+/* convertFloatToGray16Kernel over a W x H height map (texture_save.cu:80-96). */
+void ref_gray16(int W, int H, const float *h, float minv, float maxv, uint16_t *out)
+{
+    const size_t N = (size_t)W * H;
+    std::vector<float> hc(h, h + N);
+    CudaTexture<float> t(hc.data(), Vec2<int>(W, H));
+    launch(blocks_for(N), TPB, [&] { texture_save_detail::convertFloatToGray16Kernel(&t, out, minv, maxv); });
+}
+
+/* convertGrayscaleToRgbKernel over a W x H plate-id map (texture_save.cu:10-78), every cell
+ * (the reference's own launch, texture_save.cu:237, covers (W*H + 1) / 256 whole blocks only). */
+void ref_ids_rgb(int W, int H, const uint8_t *ids, uint8_t *out)
+{
+    const size_t N = (size_t)W * H;
+    std::vector<uint8_t> ic(ids, ids + N);
+    CudaTexture<uint8_t> t(ic.data(), Vec2<int>(W, H));
+    launch(blocks_for(N), TPB, [&] { texture_save_detail::convertGrayscaleToRgbKernel(&t, out); });
 }
 
 } // extern "C"

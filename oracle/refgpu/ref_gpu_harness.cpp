@@ -281,3 +281,75 @@ int refgpu_time_steps(int W, int H, const float *h_host, const uint8_t *id_host,
 }
 
 }  // extern "C"
+
+// ---- the reference's image export (oracle/_ref/ref_export.cubin, texture_save.cu) ----------------
+
+namespace {
+CUmodule g_exp = nullptr;
+CUfunction g_gray16 = nullptr, g_rgb = nullptr;
+
+// One conversion kernel over n cells: its input texture (RefTex in device memory) and output.
+int run_export(CUfunction fn, const void *in_host, size_t in_bytes, int W, int H, void *out_host,
+               size_t out_bytes, float minv, float maxv)
+{
+    void *din = nullptr, *dout = nullptr;
+    RefTex *dtex = nullptr;
+    int rc = 0;
+    if (cudaMalloc(&din, in_bytes) != cudaSuccess || cudaMalloc(&dout, out_bytes) != cudaSuccess ||
+        cudaMalloc((void **)&dtex, sizeof(RefTex)) != cudaSuccess)
+        rc = fail("cudaMalloc failed");
+    if (rc == 0) {
+        const RefTex t{din, W, H};
+        if (cudaMemcpy(dtex, &t, sizeof(t), cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(din, in_host, in_bytes, cudaMemcpyHostToDevice) != cudaSuccess)
+            rc = fail("cudaMemcpy failed");
+    }
+    if (rc == 0) {
+        const size_t n = (size_t)W * H;
+        const unsigned blocks = (unsigned)((n + 255) / 256);  // the kernels check their bounds
+        void *gray_args[] = {&dtex, &dout, &minv, &maxv};
+        void *rgb_args[] = {&dtex, &dout};
+        const CUresult r = cuLaunchKernel(fn, blocks, 1, 1, 256, 1, 1, 0, nullptr,
+                                          fn == g_gray16 ? gray_args : rgb_args, nullptr);
+        if (r != CUDA_SUCCESS) rc = fail("cuLaunchKernel failed");
+        else if (cudaMemcpy(out_host, dout, out_bytes, cudaMemcpyDeviceToHost) != cudaSuccess)
+            rc = fail("cudaMemcpy back failed");
+    }
+    cudaFree(din);
+    cudaFree(dout);
+    cudaFree(dtex);
+    return rc;
+}
+}  // namespace
+
+extern "C" {
+
+int refgpu_export_load(const char *cubin_path)
+{
+    if (g_exp) return 0;
+    RT(cudaFree(nullptr));
+    DRV(cuModuleLoad(&g_exp, cubin_path));
+    DRV(cuModuleGetFunction(&g_gray16, g_exp,
+                            "_ZN19texture_save_detail26convertFloatToGray16KernelEPK11CudaTextureIfEPtff"));
+    DRV(cuModuleGetFunction(&g_rgb, g_exp,
+                            "_ZN19texture_save_detail27convertGrayscaleToRgbKernelEPK11CudaTextureIhEPh"));
+    return 0;
+}
+
+// convertFloatToGray16Kernel over a W x H height map.
+int refgpu_gray16(const float *h, int W, int H, float minv, float maxv, uint16_t *out)
+{
+    if (!g_exp) return fail("refgpu_export_load first");
+    const size_t n = (size_t)W * H;
+    return run_export(g_gray16, h, n * 4, W, H, out, n * 2, minv, maxv);
+}
+
+// convertGrayscaleToRgbKernel over a W x H plate-id map (3 bytes per cell out).
+int refgpu_ids_rgb(const uint8_t *ids, int W, int H, uint8_t *out)
+{
+    if (!g_exp) return fail("refgpu_export_load first");
+    const size_t n = (size_t)W * H;
+    return run_export(g_rgb, ids, n, W, H, out, n * 3, 0.0f, 0.0f);
+}
+
+}  // extern "C"

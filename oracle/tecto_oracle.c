@@ -1021,3 +1021,49 @@ void or_step(int W, int H, float *h, float *w, float *s, float *flux, uint8_t *i
     if (*iteration % (uint32_t)period == 0) or_ccl(W, H, id, labels, st->step.cclConnectivity);
     *iteration += 1;
 }
+
+/* ---- image export ------------------------------------------------------------------------------ */
+
+/* convertFloatToGray16Kernel, texture_save.cu:80-96. */
+void or_gray16(size_t n, const float *h, float minv, float maxv, uint16_t *out)
+{
+    for (size_t i = 0; i < n; ++i) {
+        float norm = (h[i] - minv) / (maxv - minv);
+        norm = fminf(fmaxf(norm, 0.0f), 1.0f);
+        out[i] = (uint16_t)(norm * 65535.0f);
+    }
+}
+
+/* convertGrayscaleToRgbKernel, texture_save.cu:16-70: hue steps of 1/8 by id mod 8 plus a small
+ * offset by id / 8, saturation and value oscillating with sin / cos of id * 0.1, the standard HSV
+ * to RGB sectors (compared in double, as the reference's literals are), rounded to the nearest
+ * byte; id 255 is the background (230, 235, 240). */
+void or_plate_palette(uint8_t *rgb768)
+{
+    for (int val = 0; val < 256; ++val) {
+        uint8_t *o = rgb768 + 3 * val;
+        if (val == 255) {
+            o[0] = 230;
+            o[1] = 235;
+            o[2] = 240;
+            continue;
+        }
+        const float hue = 0.125f * (float)(val % 8) + (float)val / 8.0f / 256.0f;
+        const float sat = 0.5f + 0.5f * sinf((float)val * 0.1f);
+        const float v = 0.5f + 0.5f * cosf((float)val * 0.1f);
+        const float c = v * sat;
+        const float x = c * (1.0f - fabsf(fmodf(hue * 6.0f, 2.0f) - 1.0f));
+        const float m = v - c;
+        const double hd = hue;
+        float r, g, b;
+        if (hd < 1.0 / 6.0) { r = c; g = x; b = 0.0f; }
+        else if (hd < 2.0 / 6.0) { r = x; g = c; b = 0.0f; }
+        else if (hd < 3.0 / 6.0) { r = 0.0f; g = c; b = x; }
+        else if (hd < 4.0 / 6.0) { r = 0.0f; g = x; b = c; }
+        else if (hd < 5.0 / 6.0) { r = x; g = 0.0f; b = c; }
+        else { r = c; g = 0.0f; b = x; }
+        o[0] = (uint8_t)lroundf((r + m) * 255.0f);
+        o[1] = (uint8_t)lroundf((g + m) * 255.0f);
+        o[2] = (uint8_t)lroundf((b + m) * 255.0f);
+    }
+}

@@ -82,6 +82,11 @@ void or_step(int W, int H, float *h, float *w, float *s, float *flux, uint8_t *i
              uint32_t *div_bitmap, tecto_plate *plates, const tecto_settings *st, uint32_t seed,
              uint32_t *iteration);
 
+/* Image export (src/cuda_compute/texture_save.cu): convertFloatToGray16Kernel (:80-96) over n
+ * heights, and convertGrayscaleToRgbKernel's colour (:16-70) of every plate id as a 256 x 3 palette. */
+void or_gray16(size_t n, const float *h, float minv, float maxv, uint16_t *out);
+void or_plate_palette(uint8_t *rgb768);
+
 /* Building blocks exposed for unit tests. */
 uint32_t or_hash(uint32_t v);
 float or_simplex3(float x, float y, float z, float scale, int seed);

@@ -2,7 +2,7 @@
 
 Runs here, where the reference sources exist: `make -C oracle ref` compiles the reference's
 hot-path kernels (MarWo22/master_thesis src/cuda_compute/plate_tectonics_kernel.cu, ccl.cu,
-kernel_settings.cu) for the CPU, and oracle/ref_harness.cpp launches them with a sequential thread
+kernel_settings.cu, and the conversion kernels of texture_save.cu) for the CPU, and oracle/ref_harness.cpp launches them with a sequential thread
 emulation.  Inputs come from the engine's host-only synthetic generator (deterministic in its
 seed).  Outputs are written to tests/golden/*.npz and committed; the tests never need the
 reference itself.
@@ -199,6 +199,33 @@ def ref_ccl_cases(name):
     print("wrote", name)
 
 
+def ref_export(name):
+    """The reference's image conversions (texture_save.cu): the colour of every plate id (a 16 x 16
+    map of ids 0..255) and the 16-bit grey of heights around, at and beyond the default
+    minUpliftClamp / maxUpliftClamp range and of random heights over another range."""
+    R = O.ref()
+    ids = np.arange(256, dtype=np.uint8).reshape(16, 16)
+    rgb = np.zeros((16, 16, 3), np.uint8)
+    R.ref_ids_rgb(16, 16, P(ids), P(rgb))
+    st = T.default_settings()
+    lo, hi = float(st.kernel.minUpliftClamp), float(st.kernel.maxUpliftClamp)
+    span = hi - lo
+    edge = np.array([lo - 1.0, lo, np.nextafter(np.float32(lo), np.float32(hi)), lo + span * 0.25, lo + span * 0.5,
+                     np.nextafter(np.float32(hi), np.float32(lo)), hi, hi + 1.0, -3.0e38, 3.0e38, 0.0, -0.0],
+                    np.float32)
+    rng = np.random.default_rng(17)
+    h1 = np.concatenate([edge, rng.uniform(lo - 0.1 * span, hi + 0.1 * span, 1024 - edge.size).astype(np.float32)])
+    h1 = h1.reshape(32, 32)
+    g1 = np.zeros((32, 32), np.uint16)
+    R.ref_gray16(32, 32, P(h1), lo, hi, P(g1))
+    h2 = rng.normal(0.0, 400.0, (24, 40)).astype(np.float32)
+    g2 = np.zeros((24, 40), np.uint16)
+    R.ref_gray16(40, 24, P(h2), -1000.0, 1000.0, P(g2))
+    np.savez_compressed(OUT / f"{name}.npz", ids=ids, rgb=rgb, h1=h1, lo1=np.float32(lo), hi1=np.float32(hi), g1=g1,
+                        h2=h2, lo2=np.float32(-1000.0), hi2=np.float32(1000.0), g2=g2)
+    print("wrote", name)
+
+
 def main():
     O.build(ref=True)
     ref_step_composition("ref_steps_baseline_64x64", 64, 64, 8, 1.0, 7, "baseline", 6, 20, 0.02)
@@ -207,6 +234,7 @@ def main():
     ref_uplift_steps("ref_uplift_64x48", 64, 48, 8, 1.5, 21, 5, 12000.0)
     ref_thermal_isolated("ref_thermal_isolated_64x64", 64, 64, 13)
     ref_ccl_cases("ref_ccl_cases")
+    ref_export("ref_export")
 
 
 if __name__ == "__main__":

@@ -76,3 +76,19 @@ def test_requests_overlap_under_continuous_batching():
 def test_world_bytes_grows_with_the_grid():
     a, b = T.world_bytes(256, 256), T.world_bytes(1024, 1024)
     assert a > 256 * 256 * 90 and b > 16 * (a - 2_000_000)
+
+
+def test_output_settings_are_checked_and_dry_runs_write_nothing(tmp_path):
+    sv = T.Server(T.baseline_settings(), T.world_bytes(256, 256), dry_run=True)
+    for bad in [(tmp_path, 8, 0.0, 1.0), (tmp_path, -1, 0.0, 1.0), (None, T.SERVER_OUT_SNAPSHOT, 0.0, 1.0),
+                (tmp_path, T.SERVER_OUT_HEIGHT_PNG, 1.0, 1.0)]:
+        try:
+            sv.set_output(*bad)
+        except T.TectoError:
+            continue
+        raise AssertionError(f"accepted {bad}")
+    sv.set_output(tmp_path, T.SERVER_OUT_HEIGHT_PNG | T.SERVER_OUT_PLATES_PNG | T.SERVER_OUT_SNAPSHOT, -1.0, 1.0)
+    res, st = sv.run_trace([req(64, 64, 3, 0.0), req(32, 32, 2, 0.01)])
+    assert st.completed == 2 and all(r.status == 0 for r in res)
+    assert list(tmp_path.iterdir()) == []
+    sv.set_output(None, 0)  # off again
