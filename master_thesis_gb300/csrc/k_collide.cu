@@ -9,11 +9,38 @@ namespace {
 // Per-plate integer displacement (getPixelMovements, :248-257) and the sub-cell centre update
 // of applyPlateMovementChanges (:1871-1878), one block per world; the record before the update is
 // kept in plates_prev for the kernels of the same step.  Also resets the world's per-step
-// accretion list.
-__global__ void k_plates(const WorldDev *worlds)
+// accretion list.  With plate dynamics it first turns the sums k_plate_stats left into each
+// plate's mass, size and geometric centre (mergeAndCountSizeMass, calculatePlateCenters
+// :2191-2226: the angular means back to cells through atan2), and clears them.  The reference
+// computes no centre before its first iteration ends, so iteration 0 keeps the stored one.
+__global__ void k_plates(const WorldDev *worlds, int dynamics)
 {
     const WorldDev &wd = worlds[blockIdx.x];
     const int k = threadIdx.x;
+    if (dynamics && k < kPlates) {
+        PlateAcc &a = wd.pacc[k];
+        tecto_plate_dynamics dd = wd.dyn[k];
+        dd.mass = tecto_unfix((long long)a.mass, 1.0 / (double)kMassScale);
+        dd.size = a.size;
+        if (a.samples > 0 && wd.ctl->iteration > 0) {
+            const float n = (float)a.samples;
+            const float sx = tecto_unfix((long long)a.ang[0], 1.0 / (double)kAngScale) / n;
+            const float cx = tecto_unfix((long long)a.ang[1], 1.0 / (double)kAngScale) / n;
+            const float sy = tecto_unfix((long long)a.ang[2], 1.0 / (double)kAngScale) / n;
+            const float cy = tecto_unfix((long long)a.ang[3], 1.0 / (double)kAngScale) / n;
+            float gx = tecto_atan2f(sx, cx) * (float)wd.W / kTwoPiF;
+            float gy = tecto_atan2f(sy, cy) * (float)wd.H / kTwoPiF;
+            if (gx < 0.0f) gx += (float)wd.W;
+            if (gy < 0.0f) gy += (float)wd.H;
+            dd.geometricCenter_x = gx;
+            dd.geometricCenter_y = gy;
+        }
+        wd.dyn[k] = dd;
+        a.mass = 0ull;
+        a.ang[0] = a.ang[1] = a.ang[2] = a.ang[3] = 0ull;
+        a.size = 0;
+        a.samples = 0;
+    }
     if (k < kPlates) {
         tecto_plate p = wd.plates[k];
         wd.plates_prev[k] = p;  // the record the rest of the step sees in the reference
@@ -170,9 +197,15 @@ __global__ void k_type_matrix(const WorldDev *worlds, int cooldown, int minSize)
 
 int launch_plates(Batch &b, cudaStream_t st)
 {
-    const int rc = launch_clear_marks(b, st);  // must run before k_plates resets the list count
+    const int dyn = b.settings.step.plateDynamics;
+    if (dyn != TECTO_PLATE_DYNAMICS_OFF && dyn != TECTO_PLATE_DYNAMICS_REFERENCE) {
+        set_error("plateDynamics must be TECTO_PLATE_DYNAMICS_OFF or TECTO_PLATE_DYNAMICS_REFERENCE");
+        return TECTO_ERR_UNSUPPORTED;
+    }
+    int rc = launch_clear_marks(b, st);  // must run before k_plates resets the list count
     if (rc != TECTO_OK) return rc;
-    k_plates<<<(unsigned)b.members.size(), 256, 0, st>>>(b.d_worlds);
+    if (dyn && (rc = launch_plate_stats(b, st)) != TECTO_OK) return rc;
+    k_plates<<<(unsigned)b.members.size(), 256, 0, st>>>(b.d_worlds, dyn);
     TECTO_CUDA(cudaGetLastError());
     b.launches += 1;
     return TECTO_OK;

@@ -22,6 +22,15 @@ struct ResolveParams {
     float wts[2 * kMaxBlurRadius + 1];
     float *upl_h;      // reference uplift: processConvergence's records by virtual cell, or null
     uint8_t *upl_t;
+    float fricC, fricA, fricS;  // frictionCoefficientContinental / Accretion / Subduction
+};
+
+// Plate dynamics' view inside the resolve: velocity and mass per plate, and the block's friction
+// sums (fixed point, see PlateAcc).
+struct ResolveDyn {
+    const float *vel;
+    const float *mass;
+    unsigned long long *fric;
 };
 
 // One world's view inside the resolve kernel.
@@ -69,9 +78,11 @@ __device__ __forceinline__ void mark_accretion(const ResolveParams &p, const Res
 }
 
 // Resolve one destination cell d = (x, y); returns the new height (before uplift).
+template <bool DYN>
 __device__ __forceinline__ float resolve_cell(const ResolveParams &p, const ResolveWorld &w,
                                               const int2 *s_off, int x, int y, uint32_t d, uint32_t cv,
-                                              uint32_t seed, uint32_t iteration, uint8_t *id_out)
+                                              uint32_t seed, uint32_t iteration, uint8_t *id_out,
+                                              const ResolveDyn &dyn)
 {
     // Convergent cells also leave processConvergence's UpliftData (:501-582) for the reference
     // uplift when it is on: heightAddition, the sum of each owner pair's lower height, and typeByte.
@@ -121,6 +132,23 @@ __device__ __forceinline__ float resolve_cell(const ResolveParams &p, const Reso
         if (types[a] == 1u || types[a] == 3u) sub[PA[a]] = true;
         else if (types[a] == 2u || types[a] == 4u) sub[PB[a]] = true;
     }
+    if (DYN) {
+        // applyInelasticCollision's friction (:397-466 with applyElasticVelocityChange :371-394):
+        // per arrival, velocity x coefficient x (source height / plate mass); the coefficient is the
+        // continental one when a pair with this arrival has type 0, else the accretion one when a
+        // pair has type 3 or 4, else the subduction one
+        for (int k = 0; k < n; ++k) {
+            bool cont = false, accr = false;
+            for (int a = 0; a < pairLen; ++a) {
+                if (PA[a] != k && PB[a] != k) continue;
+                cont = cont || types[a] == 0u;
+                accr = accr || types[a] == 3u || types[a] == 4u;
+            }
+            const float coef = cont ? p.fricC : (accr ? p.fricA : p.fricS);
+            const float f = (dyn.vel[ids[k]] * coef) * (heights[k] / dyn.mass[ids[k]]);
+            atomicAdd(dyn.fric + ids[k], (unsigned long long)tecto_fix(f, kFricScale, kFricLimit));
+        }
+    }
     int owner = 0;
     for (int i = 0; i < n; ++i)
         if (!sub[i]) owner = i;
@@ -167,13 +195,15 @@ __device__ __forceinline__ float resolve_cell(const ResolveParams &p, const Reso
     return writeH;
 }
 
-template <int R>
+template <int R, bool DYN>
 __global__ __launch_bounds__(256) void k_resolve(ResolveParams p)
 {
     constexpr int SX = RX + 2 * R, SY = RY + 2 * R;
     __shared__ uint32_t s_word[SY * SX];
     __shared__ float s_tmp[(R > 0) ? SY * RX : 1];
     __shared__ int2 s_off[kPlates + 1];
+    __shared__ float s_vel[DYN ? kPlates : 1], s_mass[DYN ? kPlates : 1];
+    __shared__ unsigned long long s_fric[DYN ? kPlates : 1];
     int wi, tx, ty;
     tile_of(p.tiles[blockIdx.x], &wi, &tx, &ty);
     const WorldDev &wd = p.worlds[wi];
@@ -195,6 +225,14 @@ __global__ __launch_bounds__(256) void k_resolve(ResolveParams p)
     const int t = threadIdx.x;
     const int x0 = tx * RX, y0 = ty * RY;
     for (int i = t; i < kPlates + 1; i += 256) s_off[i] = wd.off[i];
+    if (DYN) {
+        for (int i = t; i < kPlates; i += 256) {
+            s_vel[i] = wd.plates[i].velocity;
+            s_mass[i] = wd.dyn[i].mass;
+            s_fric[i] = 0ull;
+        }
+    }
+    const ResolveDyn dyn{s_vel, s_mass, s_fric};
     for (int e = t; e < SY * SX; e += 256) {
         const int ly = e / SX, lx = e - ly * SX;
         const int gx = wrap_fast(x0 + lx - R, w.W), gy = wrap_fast(y0 + ly - R, w.H);
@@ -224,7 +262,7 @@ __global__ __launch_bounds__(256) void k_resolve(ResolveParams p)
         const uint32_t d = (uint32_t)y * (uint32_t)w.W + (uint32_t)x;
         const uint32_t cv = s_word[(ly + R) * SX + lx + R];
         uint8_t nid;
-        float hn = resolve_cell(p, w, s_off, x, y, d, cv, seed, iteration, &nid);
+        float hn = resolve_cell<DYN>(p, w, s_off, x, y, d, cv, seed, iteration, &nid, dyn);
         if (R > 0) {
             float a = 0.0f;
 #pragma unroll
@@ -233,6 +271,11 @@ __global__ __launch_bounds__(256) void k_resolve(ResolveParams p)
         }
         h_new[d] = hn;
         id_new[d] = nid;
+    }
+    if (DYN) {
+        __syncthreads();
+        for (int i = t; i < kPlates; i += 256)
+            if (s_fric[i] != 0ull) atomicAdd(&wd.pacc[i].fric, s_fric[i]);
     }
 }
 
@@ -305,6 +348,9 @@ int launch_resolve(Batch &b, cudaStream_t st)
     p.tmax = s.kernel.divergence_height_target_max;
     p.tfac = s.kernel.divergence_interpolation_factor;
     p.amount = s.step.upliftAmount;
+    p.fricC = s.kernel.frictionCoefficientContinental;
+    p.fricA = s.kernel.frictionCoefficientAccretion;
+    p.fricS = s.kernel.frictionCoefficientSubduction;
     if (s.step.upliftMode == TECTO_UPLIFT_REFERENCE) {
         p.upl_h = b.upref.upl_h;
         p.upl_t = b.upref.upl_t;
@@ -323,16 +369,28 @@ int launch_resolve(Batch &b, cudaStream_t st)
         gaussian_weights(s.step.upliftSigma, R, p.wts);
     }
     const unsigned grid = (unsigned)b.ntiles[TK_RESOLVE];
-    switch (R) {
-        case 0: k_resolve<0><<<grid, 256, 0, st>>>(p); break;
-        case 1: k_resolve<1><<<grid, 256, 0, st>>>(p); break;
-        case 2: k_resolve<2><<<grid, 256, 0, st>>>(p); break;
-        case 3: k_resolve<3><<<grid, 256, 0, st>>>(p); break;
-        case 4: k_resolve<4><<<grid, 256, 0, st>>>(p); break;
-        case 5: k_resolve<5><<<grid, 256, 0, st>>>(p); break;
-        case 6: k_resolve<6><<<grid, 256, 0, st>>>(p); break;
-        case 7: k_resolve<7><<<grid, 256, 0, st>>>(p); break;
-        default: k_resolve<8><<<grid, 256, 0, st>>>(p); break;
+    if (s.step.plateDynamics == TECTO_PLATE_DYNAMICS_REFERENCE) {
+        switch (R) {
+            case 0: k_resolve<0, true><<<grid, 256, 0, st>>>(p); break;
+            case 1: k_resolve<1, true><<<grid, 256, 0, st>>>(p); break;
+            case 2: k_resolve<2, true><<<grid, 256, 0, st>>>(p); break;
+            case 3: k_resolve<3, true><<<grid, 256, 0, st>>>(p); break;
+            case 4: k_resolve<4, true><<<grid, 256, 0, st>>>(p); break;
+            case 5: k_resolve<5, true><<<grid, 256, 0, st>>>(p); break;
+            case 6: k_resolve<6, true><<<grid, 256, 0, st>>>(p); break;
+            case 7: k_resolve<7, true><<<grid, 256, 0, st>>>(p); break;
+            default: k_resolve<8, true><<<grid, 256, 0, st>>>(p); break;
+        }
+    } else switch (R) {
+        case 0: k_resolve<0, false><<<grid, 256, 0, st>>>(p); break;
+        case 1: k_resolve<1, false><<<grid, 256, 0, st>>>(p); break;
+        case 2: k_resolve<2, false><<<grid, 256, 0, st>>>(p); break;
+        case 3: k_resolve<3, false><<<grid, 256, 0, st>>>(p); break;
+        case 4: k_resolve<4, false><<<grid, 256, 0, st>>>(p); break;
+        case 5: k_resolve<5, false><<<grid, 256, 0, st>>>(p); break;
+        case 6: k_resolve<6, false><<<grid, 256, 0, st>>>(p); break;
+        case 7: k_resolve<7, false><<<grid, 256, 0, st>>>(p); break;
+        default: k_resolve<8, false><<<grid, 256, 0, st>>>(p); break;
     }
     k_flip<<<dim3((kDivWords + 255) / 256, (unsigned)b.members.size()), 256, 0, st>>>(b.d_worlds);
     TECTO_CUDA(cudaGetLastError());
@@ -344,6 +402,10 @@ int launch_resolve(Batch &b, cudaStream_t st)
 
 int launch_finish(Batch &b, cudaStream_t st)
 {
+    if (b.settings.step.plateDynamics == TECTO_PLATE_DYNAMICS_REFERENCE) {
+        const int rc = launch_plate_motion(b, st);  // executeIteration: before applyAccretion
+        if (rc != TECTO_OK) return rc;
+    }
     k_finish<<<dim3(4, (unsigned)b.members.size()), 256, 0, st>>>(b.d_worlds, b.cur_h, b.cur_id,
                                                                    b.settings.kernel.continentalCrustThreshold);
     TECTO_CUDA(cudaGetLastError());

@@ -151,7 +151,8 @@ const Field kKernelFields[] = {
 #define SI(n) {#n, 'i', offsetof(tecto_step_settings, n)}
 const Field kStepFields[] = {SI(hydraulicIterations), SF(hydraulicDt), SI(thermalIterations),
                              SI(upliftMode), SF(upliftAmount), SF(upliftSigma), SI(upliftRadius),
-                             SI(cclConnectivity), SI(sortRadixBits), SI(hydraulicTile), SI(thermalTile)};
+                             SI(cclConnectivity), SI(sortRadixBits), SI(hydraulicTile), SI(thermalTile),
+                             SI(plateDynamics)};
 #undef SF
 #undef SI
 const Field kSimFields[] = {{"numStartingPlates", 'i', offsetof(tecto_simulation_settings, numStartingPlates)},

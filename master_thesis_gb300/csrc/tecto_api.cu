@@ -144,7 +144,8 @@ size_t world_footprint(int W, int H)
     L.add(N * 4); L.add(N * 4); L.add(N * 4); L.add(N * 8); L.add(N * 4); L.add(N * 8); L.add(N * 4); L.add(N);
     L.add(kPairs); L.add(kDivWords * 4); L.add(kDivWords * 4); L.add(kPairs * sizeof(PairCounts));
     L.add(kPlates * sizeof(tecto_plate)); L.add(kPlates * sizeof(tecto_plate));
-    L.add((kPlates + 1) * sizeof(int2)); L.add(sizeof(Control));
+    L.add((kPlates + 1) * sizeof(int2)); L.add(kPlates * sizeof(tecto_plate_dynamics));
+    L.add(kPlates * sizeof(PlateAcc)); L.add(sizeof(Control));
     // its share of a batch's sort: key/value ping-pong plus the scratch of the widest digit choice
     size_t scratch = 0;
     for (int rb = 8; rb <= kMaxRadixBits; ++rb)
@@ -210,6 +211,8 @@ int tecto_world_create(const tecto_settings *settings, int width, int height, ui
     const size_t o_pl = L.add(kPlates * sizeof(tecto_plate));
     const size_t o_plp = L.add(kPlates * sizeof(tecto_plate));
     const size_t o_off = L.add((kPlates + 1) * sizeof(int2));
+    const size_t o_dyn = L.add(kPlates * sizeof(tecto_plate_dynamics));
+    const size_t o_pacc = L.add(kPlates * sizeof(PlateAcc));
     const size_t o_ctl = L.add(sizeof(Control));
     cudaError_t e = cudaMalloc(&w->arena, L.total);
     if (e != cudaSuccess) {
@@ -248,6 +251,10 @@ int tecto_world_create(const tecto_settings *settings, int width, int height, ui
     d.plates = (tecto_plate *)(base + o_pl);
     d.plates_prev = (tecto_plate *)(base + o_plp);
     d.off = (int2 *)(base + o_off);
+    d.dyn = (tecto_plate_dynamics *)(base + o_dyn);
+    d.pacc = (PlateAcc *)(base + o_pacc);
+    d.pressure = nullptr;
+    d.pw = d.ph = 0;
     d.ctl = (Control *)(base + o_ctl);
     e = cudaMemset(w->arena, 0, L.total);
     if (e == cudaSuccess) {
@@ -281,6 +288,8 @@ int tecto_world_destroy(tecto_world *w)
     }
     if (w->arena) cudaFree(w->arena);
     w->arena = nullptr;
+    if (w->pressure) cudaFree(w->pressure);
+    w->pressure = nullptr;
     delete w;
     return TECTO_OK;
 }
@@ -413,6 +422,8 @@ int tecto_world_init_synthetic_device(tecto_world *w, int P, float velRange, uin
     TECTO_CUDA(cudaMemcpyAsync(dsx, sx.data(), P * sizeof(float), cudaMemcpyHostToDevice, st));
     TECTO_CUDA(cudaMemcpyAsync(dsy, sy.data(), P * sizeof(float), cudaMemcpyHostToDevice, st));
     TECTO_CUDA(cudaMemcpyAsync(d.plates, pl.data(), sizeof(tecto_plate) * kPlates, cudaMemcpyHostToDevice, st));
+    TECTO_CUDA(cudaMemsetAsync(d.dyn, 0, sizeof(tecto_plate_dynamics) * kPlates, st));  // fresh PlateData
+    TECTO_CUDA(cudaMemsetAsync(d.pacc, 0, sizeof(PlateAcc) * kPlates, st));
     Control c{};
     c.seed = w->seed;
     TECTO_CUDA(cudaMemcpyAsync(d.ctl, &c, sizeof(c), cudaMemcpyHostToDevice, st));
@@ -489,6 +500,8 @@ int tecto_world_init_synthetic(tecto_world *w, int P, float velRange, uint64_t g
     TECTO_CUDA(cudaMemcpyAsync(d.h[w->cur_h], h.data(), N * 4, cudaMemcpyHostToDevice, st));
     TECTO_CUDA(cudaMemcpyAsync(d.id[w->cur_id], id.data(), N, cudaMemcpyHostToDevice, st));
     TECTO_CUDA(cudaMemcpyAsync(d.plates, pl.data(), sizeof(tecto_plate) * kPlates, cudaMemcpyHostToDevice, st));
+    TECTO_CUDA(cudaMemsetAsync(d.dyn, 0, sizeof(tecto_plate_dynamics) * kPlates, st));  // fresh PlateData
+    TECTO_CUDA(cudaMemsetAsync(d.pacc, 0, sizeof(PlateAcc) * kPlates, st));
     Control c{};
     c.seed = w->seed;
     TECTO_CUDA(cudaMemcpyAsync(d.ctl, &c, sizeof(c), cudaMemcpyHostToDevice, st));
@@ -600,6 +613,60 @@ int tecto_world_get_plates(tecto_world *w, tecto_plate *plates, int count, tecto
     cudaStream_t st = (cudaStream_t)stream;
     TECTO_CUDA(cudaMemcpyAsync(plates, w->dev.plates, sizeof(tecto_plate) * count, cudaMemcpyDeviceToHost, st));
     TECTO_CUDA(cudaStreamSynchronize(st));
+    return TECTO_OK;
+}
+
+int tecto_world_set_plate_dynamics(tecto_world *w, const tecto_plate_dynamics *plates, int count,
+                                   tecto_stream_t stream)
+{
+    int rc = check_world(w);
+    if (rc != TECTO_OK) return rc;
+    if (!plates || count < 0 || count > kPlates) return TECTO_ERR_INVALID;
+    if ((rc = bind_device(w)) != TECTO_OK) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    TECTO_CUDA(cudaMemcpyAsync(w->dev.dyn, plates, sizeof(tecto_plate_dynamics) * count, cudaMemcpyHostToDevice, st));
+    TECTO_CUDA(cudaStreamSynchronize(st));
+    return TECTO_OK;
+}
+
+int tecto_world_get_plate_dynamics(tecto_world *w, tecto_plate_dynamics *plates, int count, tecto_stream_t stream)
+{
+    int rc = check_world(w);
+    if (rc != TECTO_OK) return rc;
+    if (!plates || count < 0 || count > kPlates) return TECTO_ERR_INVALID;
+    if ((rc = bind_device(w)) != TECTO_OK) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    TECTO_CUDA(cudaMemcpyAsync(plates, w->dev.dyn, sizeof(tecto_plate_dynamics) * count, cudaMemcpyDeviceToHost, st));
+    TECTO_CUDA(cudaStreamSynchronize(st));
+    return TECTO_OK;
+}
+
+int tecto_world_set_asthenosphere(tecto_world *w, const float *pressure, int pw, int ph, tecto_stream_t stream)
+{
+    int rc = check_world(w);
+    if (rc != TECTO_OK) return rc;
+    if (pressure && (pw < 1 || ph < 1 || (size_t)pw * (size_t)ph > ((size_t)1 << 30))) {
+        set_error("tecto_world_set_asthenosphere: invalid texture size");
+        return TECTO_ERR_INVALID;
+    }
+    if ((rc = bind_device(w)) != TECTO_OK) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    TECTO_CUDA(cudaStreamSynchronize(st));  // no step in flight reads the old texture
+    TECTO_CUDA(cudaDeviceSynchronize());
+    if (w->pressure) cudaFree(w->pressure);
+    w->pressure = nullptr;
+    w->pw = w->ph = 0;
+    if (pressure) {
+        const size_t bytes = (size_t)pw * (size_t)ph * 4;
+        TECTO_CUDA(cudaMalloc(&w->pressure, bytes));
+        w->pw = pw;
+        w->ph = ph;
+        TECTO_CUDA(cudaMemcpy(w->pressure, pressure, bytes, cudaMemcpyHostToDevice));
+    }
+    w->dev.pressure = w->pressure;
+    w->dev.pw = w->pw;
+    w->dev.ph = w->ph;
+    if (w->in_batch) w->in_batch->dirty = true;  // the batch's device table holds the pointer
     return TECTO_OK;
 }
 

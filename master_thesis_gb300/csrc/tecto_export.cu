@@ -195,8 +195,11 @@ int write_file(const char *path, const void *data, size_t n)
 }
 
 // ---- snapshots ----------------------------------------------------------------------------------
+// File: SnapHeader, tecto_settings, the fields of snap_fields() in that order, the 255 plate records,
+// the 255 plate dynamics records, then the asthenosphere pressure texture (pw x ph floats), all in
+// the host's byte order.
 
-constexpr char kMagic[8] = {'T', 'E', 'C', 'T', 'O', 'S', 'N', '1'};
+constexpr char kMagic[8] = {'T', 'E', 'C', 'T', 'O', 'S', 'N', '2'};
 
 struct SnapHeader {
     char magic[8];
@@ -204,6 +207,7 @@ struct SnapHeader {
     int32_t width, height;
     uint32_t seed, iteration;
     uint64_t cells;
+    int32_t pw, ph;  // asthenosphere pressure texture, 0 x 0 when there is none
 };
 
 struct SnapField {
@@ -313,6 +317,8 @@ int tecto_world_save_snapshot(tecto_world *w, const char *path, tecto_stream_t s
     hd.seed = w->seed;
     hd.iteration = w->iteration;
     hd.cells = w->N;
+    hd.pw = w->pw;
+    hd.ph = w->ph;
     std::vector<uint8_t> buf(sizeof(hd) + sizeof(tecto_settings));
     std::memcpy(buf.data(), &hd, sizeof(hd));
     std::memcpy(buf.data() + sizeof(hd), &w->settings, sizeof(tecto_settings));
@@ -324,9 +330,20 @@ int tecto_world_save_snapshot(tecto_world *w, const char *path, tecto_stream_t s
     }
     std::vector<tecto_plate> plates(kPlates);
     if ((rc = tecto_world_get_plates(w, plates.data(), kPlates, stream)) != TECTO_OK) return rc;
-    const size_t at = buf.size();
+    size_t at = buf.size();
     buf.resize(at + plates.size() * sizeof(tecto_plate));
     std::memcpy(buf.data() + at, plates.data(), plates.size() * sizeof(tecto_plate));
+    std::vector<tecto_plate_dynamics> dyn(kPlates);
+    if ((rc = tecto_world_get_plate_dynamics(w, dyn.data(), kPlates, stream)) != TECTO_OK) return rc;
+    at = buf.size();
+    buf.resize(at + dyn.size() * sizeof(tecto_plate_dynamics));
+    std::memcpy(buf.data() + at, dyn.data(), dyn.size() * sizeof(tecto_plate_dynamics));
+    if (w->pressure) {
+        at = buf.size();
+        const size_t bytes = (size_t)w->pw * (size_t)w->ph * 4;
+        buf.resize(at + bytes);
+        TECTO_CUDA(cudaMemcpy(buf.data() + at, w->pressure, bytes, cudaMemcpyDeviceToHost));
+    }
     return write_file(path, buf.data(), buf.size());
 }
 
@@ -369,9 +386,11 @@ int tecto_world_load_snapshot(tecto_world *w, const char *path, tecto_stream_t s
     const bool read = size > 0 && std::fread(buf.data(), 1, buf.size(), f) == buf.size();
     std::fclose(f);
     SnapHeader hd{};
-    size_t need = sizeof(hd) + sizeof(tecto_settings) + kPlates * sizeof(tecto_plate);
+    size_t need = sizeof(hd) + sizeof(tecto_settings) + kPlates * (sizeof(tecto_plate) + sizeof(tecto_plate_dynamics));
     if (read && buf.size() >= sizeof(hd)) std::memcpy(&hd, buf.data(), sizeof(hd));
     for (const SnapField &fl : snap_fields((size_t)hd.cells)) need += fl.bytes;
+    if (hd.pw < 0 || hd.ph < 0 || (size_t)hd.pw * (size_t)hd.ph > ((size_t)1 << 30)) need = 0;
+    else need += (size_t)hd.pw * (size_t)hd.ph * 4;
     if (!read || std::memcmp(hd.magic, kMagic, 8) != 0 || hd.header_bytes != sizeof(SnapHeader) ||
         hd.settings_bytes != sizeof(tecto_settings) || buf.size() != need) {
         set_error(std::string(path) + " is not a snapshot of this engine version");
@@ -391,6 +410,16 @@ int tecto_world_load_snapshot(tecto_world *w, const char *path, tecto_stream_t s
         at += fl.bytes;
     }
     if ((rc = tecto_world_set_plates(w, (const tecto_plate *)(buf.data() + at), kPlates, stream)) != TECTO_OK)
+        return rc;
+    at += kPlates * sizeof(tecto_plate);
+    std::vector<tecto_plate_dynamics> dyn(kPlates);
+    std::memcpy(dyn.data(), buf.data() + at, kPlates * sizeof(tecto_plate_dynamics));
+    if ((rc = tecto_world_set_plate_dynamics(w, dyn.data(), kPlates, stream)) != TECTO_OK) return rc;
+    at += kPlates * sizeof(tecto_plate_dynamics);
+    std::vector<float> pressure((size_t)hd.pw * (size_t)hd.ph);
+    if (!pressure.empty()) std::memcpy(pressure.data(), buf.data() + at, pressure.size() * 4);
+    if ((rc = tecto_world_set_asthenosphere(w, pressure.empty() ? nullptr : pressure.data(), hd.pw, hd.ph,
+                                            stream)) != TECTO_OK)
         return rc;
     if ((rc = tecto_world_set_iteration(w, hd.iteration)) != TECTO_OK) return rc;
     w->seed = hd.seed;

@@ -71,6 +71,25 @@ struct SortScratch {
     int radix_bits;      // digit width, 8..kMaxRadixBits
 };
 
+// Per-plate sums of plate dynamics, in 64-bit fixed point so that the order of the atomic adds
+// does not change the bits: mass (heights x 2^16), the angular centre sums (sin / cos x 2^32) and the
+// collision friction (x 2^40).  Consumed and cleared within each step.
+struct PlateAcc {
+    unsigned long long mass;
+    unsigned long long ang[4];  // sin x, cos x, sin y, cos y of the sampled cells
+    unsigned long long fric;
+    int size;
+    int samples;
+};
+
+constexpr float kMassScale = 65536.0f;             // 2^16
+constexpr float kMassLimit = 1099511627776.0f;     // |h| clamp before scaling, 2^40
+constexpr float kAngScale = 4294967296.0f;         // 2^32
+constexpr float kFricScale = 1099511627776.0f;     // 2^40
+constexpr float kFricLimit = 4194304.0f;           // |friction term| clamp, 2^22
+constexpr int kStatTileX = 256, kStatTileY = 64;   // TK_STATS tile
+constexpr float kTwoPiF = 6.28318548202514648f;    // CURAND_2PI as a float
+
 // Device descriptor of one world (one cudaMalloc'd arena per world, structure of arrays).
 struct WorldDev {
     int W, H;
@@ -96,6 +115,10 @@ struct WorldDev {
     tecto_plate *plates;    // [kPlates]
     tecto_plate *plates_prev;  // [kPlates] plate records before this step's centre update
     int2 *off;              // [kPlates + 1] this step's integer displacement per plate
+    tecto_plate_dynamics *dyn;  // [kPlates] plate dynamics records
+    PlateAcc *pacc;         // [kPlates] plate dynamics sums of the current step
+    const float *pressure;  // asthenosphere pressure texture (pw x ph), or null
+    int pw, ph;
     Control *ctl;
 };
 
@@ -120,7 +143,7 @@ struct UpliftRefScratch {
 };
 
 // Phase work lists.
-enum TileKind { TK_RESOLVE = 0, TK_THERMAL, TK_HYDRO, TK_CCL, TK_COUNT };
+enum TileKind { TK_RESOLVE = 0, TK_THERMAL, TK_HYDRO, TK_CCL, TK_STATS, TK_COUNT };
 
 // One batch: members, their device table, work lists and the batch-level buffers.
 struct Batch {
@@ -178,6 +201,8 @@ struct tecto_world {
     tecto::WorldDev dev{};         // host copy of the device descriptor
     tecto::Batch *own = nullptr;   // private batch of one, for stepping alone
     tecto::Batch *in_batch = nullptr;  // the batch it currently belongs to (own or public)
+    float *pressure = nullptr;     // asthenosphere pressure texture (own allocation), or null
+    int pw = 0, ph = 0;
 };
 
 struct tecto_batch {
@@ -265,6 +290,10 @@ int launch_resolve(Batch &b, cudaStream_t st);
 int launch_thermal(Batch &b, int iterations, cudaStream_t st);
 int launch_hydraulic(Batch &b, int iterations, float dt, cudaStream_t st);
 int launch_finish(Batch &b, cudaStream_t st);
+// plate dynamics (TECTO_PLATE_DYNAMICS_REFERENCE): per-plate sums at the start of a step, and
+// applyPlateMovementChanges at its end
+int launch_plate_stats(Batch &b, cudaStream_t st);
+int launch_plate_motion(Batch &b, cudaStream_t st);
 int launch_clear_marks(Batch &b, cudaStream_t st);
 int launch_bump_iteration(Batch &b, cudaStream_t st);
 // due_only: skip worlds whose step counter is not a multiple of iterationsForCCL

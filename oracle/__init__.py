@@ -119,6 +119,13 @@ def lib() -> C.CDLL:
         L.or_accretion.argtypes = [C.c_int, C.c_int, V, V, V, V]
         L.or_ccl.argtypes = [C.c_int, C.c_int, V, V, C.c_int]
         L.or_step.argtypes = [C.c_int, C.c_int, V, V, V, V, V, V, V, V, V, V, V, V, C.c_uint32, V]
+        L.or_step_dyn.argtypes = [C.c_int, C.c_int, V, V, V, V, V, V, V, V, V, V, V, V, V, C.c_int, C.c_int, V,
+                                  C.c_uint32, V]
+        L.or_resolve_dyn.argtypes = [C.c_int, C.c_int, V, V, V, V, V, V, V, V, C.c_uint32, C.c_uint32, V, V, V,
+                                     V, V, V, V, V]
+        L.or_plate_stats.argtypes = [C.c_int, C.c_int, V, V, C.c_uint32, V]
+        L.or_curl_at.argtypes = [V, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, V, V]
+        L.or_plate_motion.argtypes = [C.c_int, C.c_int, V, V, V, V, C.c_int, C.c_int, V]
         L.or_hash.argtypes = [C.c_uint32]
         L.or_hash.restype = C.c_uint32
         L.or_simplex3.argtypes = [C.c_float] * 4 + [C.c_int]
@@ -162,6 +169,10 @@ def ref() -> C.CDLL:
         L.ref_accretion.argtypes = [C.c_int, C.c_int, V, V, V]
         L.ref_ccl.argtypes = [C.c_int, C.c_int, V, V]
         L.ref_gray16.argtypes = [C.c_int, C.c_int, V, C.c_float, C.c_float, V]
+        L.ref_collision_friction.argtypes = [C.c_int, C.c_int, V, V, V, V, V, V, V, C.c_int, C.c_uint, V]
+        L.ref_plate_centres.argtypes = [C.c_int, C.c_int, V, V]
+        L.ref_curl.argtypes = [C.c_int, C.c_int, V, C.c_int, C.c_int, V]
+        L.ref_plate_motion.argtypes = [C.c_int, C.c_int, V, V, V, V]
         L.ref_ids_rgb.argtypes = [C.c_int, C.c_int, V, V]
         _r = L
     return _r
@@ -239,6 +250,33 @@ def log10f(x: float) -> float:
     return lib().or_log10f(x)
 
 
+def plate_stats(h, ids, iteration, dyn=None):
+    """or_plate_stats: mass, size and geometric centre per plate (updates a copy of dyn)."""
+    from master_thesis_gb300 import MAX_PLATES, PLATE_DYNAMICS_DTYPE
+    H, W = h.shape
+    out = np.zeros(MAX_PLATES, PLATE_DYNAMICS_DTYPE) if dyn is None else dyn.copy()
+    lib().or_plate_stats(W, H, _P(np.ascontiguousarray(h, np.float32)), _P(np.ascontiguousarray(ids, np.uint8)),
+                         iteration, _P(out))
+    return out
+
+
+def curl_at(pressure, W, H, cx, cy):
+    pr = np.ascontiguousarray(pressure, np.float32)
+    ox, oy = C.c_float(), C.c_float()
+    lib().or_curl_at(_P(pr), pr.shape[1], pr.shape[0], W, H, cx, cy, C.byref(ox), C.byref(oy))
+    return ox.value, oy.value
+
+
+def plate_motion(W, H, plates, dyn, fric, pressure, settings):
+    """or_plate_motion on copies: returns (plates, dyn)."""
+    pl, dd = plates.copy(), dyn.copy()
+    fr = np.ascontiguousarray(fric, np.int64)
+    pr = None if pressure is None else np.ascontiguousarray(pressure, np.float32)
+    pw, ph = (pr.shape[1], pr.shape[0]) if pr is not None else (0, 0)
+    lib().or_plate_motion(W, H, _P(pl), _P(dd), _P(fr), _P(pr), pw, ph, C.addressof(settings.kernel))
+    return pl, dd
+
+
 def gray16(h, minv, maxv):
     """convertFloatToGray16Kernel (texture_save.cu:80-96) on the CPU."""
     h = np.ascontiguousarray(h, np.float32)
@@ -303,8 +341,15 @@ class OracleWorld:
         self.seed = seed
         self.iteration = C.c_uint32(0)
 
+        from master_thesis_gb300 import MAX_PLATES, PLATE_DYNAMICS_DTYPE
+        self.dyn = np.zeros(MAX_PLATES, PLATE_DYNAMICS_DTYPE)
+        self.pressure = None
+
     def step(self, n: int = 1) -> None:
+        pr = self.pressure
+        pw, ph = (pr.shape[1], pr.shape[0]) if pr is not None else (0, 0)
         for _ in range(n):
-            lib().or_step(self.W, self.H, _P(self.h), _P(self.w), _P(self.s), _P(self.flux), _P(self.id),
-                          _P(self.labels), _P(self.word), _P(self.acc), _P(self.bitmap), _P(self.div),
-                          _P(self.plates), C.addressof(self.settings), self.seed, C.byref(self.iteration))
+            lib().or_step_dyn(self.W, self.H, _P(self.h), _P(self.w), _P(self.s), _P(self.flux), _P(self.id),
+                              _P(self.labels), _P(self.word), _P(self.acc), _P(self.bitmap), _P(self.div),
+                              _P(self.plates), _P(self.dyn), _P(pr), pw, ph, C.addressof(self.settings),
+                              self.seed, C.byref(self.iteration))

@@ -294,4 +294,106 @@ void ref_ids_rgb(int W, int H, const uint8_t *ids, uint8_t *out)
     launch(blocks_for(N), TPB, [&] { texture_save_detail::convertGrayscaleToRgbKernel(&t, out); });
 }
 
+/* Plate dynamics, the reference's kernels on host arrays. */
+
+/* processCollisions' CollisionVelocityChanges::frictionLoss per plate, with plate masses mass[255]
+ * (plate_tectonics_kernel.cu:371-466); the other outputs of the step are discarded. */
+void ref_collision_friction(int W, int H, const uint8_t *id_old, const float *h_old, const uint32_t *word,
+                            const tecto_plate *plates, const float *mass, const uint8_t *type_bitmap,
+                            const uint32_t *div_bitmap, int seed, unsigned iteration, float *friction)
+{
+    const size_t N = (size_t)W * H;
+    std::vector<uint8_t> idc(id_old, id_old + N), idn(N), acc(N);
+    std::vector<float> hc(h_old, h_old + N), hn(N);
+    std::vector<uint32_t> wc(word, word + N), div(div_bitmap, div_bitmap + NUM_WORDS_TRIANGLE_SINGLE_BITS);
+    std::vector<uint8_t> bm(type_bitmap, type_bitmap + NUM_TRIANGLE_ENTRIES);
+    auto pd = make_plates(plates);
+    for (unsigned k = 0; k < MAX_PLATE_COUNT; ++k) pd[k].mass = mass[k];
+    std::vector<uint32_t> hasDiv(NUM_WORDS_TRIANGLE_SINGLE_BITS, 0);
+    std::vector<UpliftData> up(N);
+    std::vector<CollisionVelocityChanges> vchg(MAX_PLATE_COUNT);
+    CudaTexture<uint8_t> tId(idc.data(), Vec2<int>(W, H)), tIdNew(idn.data(), Vec2<int>(W, H)),
+        tAcc(acc.data(), Vec2<int>(W, H));
+    CudaTexture<float> tH(hc.data(), Vec2<int>(W, H)), tHNew(hn.data(), Vec2<int>(W, H));
+    CudaTexture<uint32_t> tWord(wc.data(), Vec2<int>(W, H));
+    CudaTexture<UpliftData> tUp(up.data(), Vec2<int>(W, H));
+    const PlateTexturesRead rd = {&tId, &tH, pd.data()};
+    const PlateTexturesWrite wr = {&tIdNew, &tHNew};
+    const NoiseParameters np = {seed, iteration};
+    launch(blocks_for(N), TPB, [&] {
+        processCollisions(rd, &tWord, div.data(), bm.data(), wr, hasDiv.data(), &tUp, &tAcc, vchg.data(), np);
+    });
+    for (unsigned k = 0; k < MAX_PLATE_COUNT; ++k) friction[k] = vchg[k].frictionLoss;
+}
+
+/* accumulatePlateAngularCoords + calculatePlateCenters (:2154-2226): centre_xy[2 * plate + axis];
+ * plates without samples keep the value passed in. */
+void ref_plate_centres(int W, int H, const uint8_t *ids, float *centre_xy)
+{
+    const size_t N = (size_t)W * H;
+    std::vector<uint8_t> ic(ids, ids + N);
+    std::vector<float4> sums(MAX_PLATE_COUNT, float4{0, 0, 0, 0});
+    std::vector<int> counts(MAX_PLATE_COUNT, 0);
+    std::vector<PlateData> pd(MAX_PLATE_COUNT);
+    for (unsigned k = 0; k < MAX_PLATE_COUNT; ++k)
+        pd[k].geometricCenter = Vec2<float>(centre_xy[2 * k], centre_xy[2 * k + 1]);
+    CudaTexture<uint8_t> tId(ic.data(), Vec2<int>(W, H));
+    CudaTexture<float4> tSums(sums.data(), Vec2<int>(MAX_PLATE_COUNT, 1));
+    CudaTexture<int> tCounts(counts.data(), Vec2<int>(MAX_PLATE_COUNT, 1));
+    launch(blocks_for(N), TPB, [&] { accumulatePlateAngularCoords(&tId, &tSums, &tCounts); });
+    launch(MAX_PLATE_COUNT, 1, [&] { calculatePlateCenters(&tId, &tSums, &tCounts, pd.data()); });
+    for (unsigned k = 0; k < MAX_PLATE_COUNT; ++k) {
+        centre_xy[2 * k] = pd[k].geometricCenter.x;
+        centre_xy[2 * k + 1] = pd[k].geometricCenter.y;
+    }
+}
+
+/* computeCurl (:2788-2822): the W x H asthenosphere field (x, y per cell) of a pw x ph pressure
+ * texture. */
+void ref_curl(int pw, int ph, const float *pressure, int W, int H, float *curl_xy)
+{
+    std::vector<float> pc(pressure, pressure + (size_t)pw * ph);
+    std::vector<Vec2<float>> out((size_t)W * H);
+    CudaTexture<float> tP(pc.data(), Vec2<int>(pw, ph));
+    CudaTexture<Vec2<float>> tC(out.data(), Vec2<int>(W, H));
+    launch(blocks_for((size_t)W * H), TPB, [&] { computeCurl(&tP, &tC); });
+    for (size_t i = 0; i < out.size(); ++i) {
+        curl_xy[2 * i] = out[i].x;
+        curl_xy[2 * i + 1] = out[i].y;
+    }
+}
+
+/* applyPlateMovementChanges (:1863-1925) over the 255 plates: plates (velocity, direction,
+ * pixelCenter) and dyn (velocitySmoothed, directionSmoothed, geometricCenter, mergeWaitTime) are
+ * updated in place; friction[255] is CollisionVelocityChanges::frictionLoss; curl_xy the W x H
+ * asthenosphere field. */
+void ref_plate_motion(int W, int H, tecto_plate *plates, tecto_plate_dynamics *dyn, const float *friction,
+                      const float *curl_xy)
+{
+    auto pd = make_plates(plates);
+    std::vector<CollisionVelocityChanges> vchg(MAX_PLATE_COUNT);
+    for (unsigned k = 0; k < MAX_PLATE_COUNT; ++k) {
+        pd[k].velocitySmoothed = dyn[k].velocitySmoothed;
+        pd[k].directionSmoothed = Vec2<float>(dyn[k].directionSmoothed_x, dyn[k].directionSmoothed_y);
+        pd[k].geometricCenter = Vec2<float>(dyn[k].geometricCenter_x, dyn[k].geometricCenter_y);
+        pd[k].mergeWaitTime = dyn[k].mergeWaitTime;
+        vchg[k].frictionLoss = friction[k];
+    }
+    std::vector<Vec2<float>> curl((size_t)W * H);
+    for (size_t i = 0; i < curl.size(); ++i) curl[i] = Vec2<float>(curl_xy[2 * i], curl_xy[2 * i + 1]);
+    CudaTexture<Vec2<float>> tC(curl.data(), Vec2<int>(W, H));
+    launch(1, 256, [&] { applyPlateMovementChanges(pd.data(), vchg.data(), &tC); });
+    for (unsigned k = 0; k < MAX_PLATE_COUNT; ++k) {
+        plates[k].velocity = pd[k].velocity;
+        plates[k].direction_x = pd[k].direction.x;
+        plates[k].direction_y = pd[k].direction.y;
+        plates[k].pixelCenter_x = pd[k].pixelCenter.x;
+        plates[k].pixelCenter_y = pd[k].pixelCenter.y;
+        dyn[k].velocitySmoothed = pd[k].velocitySmoothed;
+        dyn[k].directionSmoothed_x = pd[k].directionSmoothed.x;
+        dyn[k].directionSmoothed_y = pd[k].directionSmoothed.y;
+        dyn[k].mergeWaitTime = pd[k].mergeWaitTime;
+    }
+}
+
 } // extern "C"

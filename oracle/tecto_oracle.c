@@ -12,6 +12,13 @@
 #include <string.h>
 
 #define NPLATE 255u
+/* plate dynamics' fixed-point sums (the engine uses the same scales) */
+#define OR_MASS_SCALE 65536.0f
+#define OR_MASS_LIMIT 1099511627776.0f
+#define OR_ANG_SCALE 4294967296.0f
+#define OR_FRIC_SCALE 1099511627776.0f
+#define OR_FRIC_LIMIT 4194304.0f
+#define OR_TWO_PI_F 6.28318548202514648f
 
 /* ---- addressing --------------------------------------------------------------------- */
 
@@ -357,6 +364,22 @@ void or_resolve_ex(int W, int H, const uint8_t *id_old, const float *h_old, cons
                    const tecto_settings *st, uint32_t seed, uint32_t iteration, float *h_new,
                    uint8_t *id_new, uint8_t *acc, float *up_h, uint8_t *up_t)
 {
+    or_resolve_dyn(W, H, id_old, h_old, word, off_x, off_y, bm, div_bitmap, st, seed, iteration, h_new, id_new,
+                   acc, up_h, up_t, NULL, NULL, NULL);
+}
+
+/* or_resolve_ex plus, when fric is not NULL, each plate's collision friction of the step: for every
+ * arrival at a convergent cell, applyElasticVelocityChange's term (plate_tectonics_kernel.cu:371-394)
+ * velocity x coefficient x (source height / plate mass), the coefficient chosen as
+ * applyInelasticCollision does (:397-466: continental when a pair with this arrival has type 0,
+ * accretion when one has type 3 or 4, else subduction), summed in fixed point (x 2^40) in fric[plate].
+ * plates: the records the resolve sees (velocity); dyn: the step's plate masses. */
+void or_resolve_dyn(int W, int H, const uint8_t *id_old, const float *h_old, const uint32_t *word,
+                    const int32_t *off_x, const int32_t *off_y, const uint8_t *bm, uint32_t *div_bitmap,
+                    const tecto_settings *st, uint32_t seed, uint32_t iteration, float *h_new,
+                    uint8_t *id_new, uint8_t *acc, float *up_h, uint8_t *up_t, const tecto_plate *plates,
+                    const tecto_plate_dynamics *dyn, int64_t *fric)
+{
     const tecto_kernel_settings *ks = &st->kernel;
     const size_t N = (size_t)W * (size_t)H;
     uint32_t has_div[TECTO_NUM_DIV_WORDS];
@@ -416,6 +439,21 @@ void or_resolve_ex(int W, int H, const uint8_t *id_old, const float *h_old, cons
         for (int a = 0; a < pairLen; ++a) {
             if (types[a] == 1 || types[a] == 3) sub[PL[a][0]] = 1;
             else if (types[a] == 2 || types[a] == 4) sub[PL[a][1]] = 1;
+        }
+        if (fric) {
+            for (int k = 0; k < n; ++k) {
+                int cont = 0, accr = 0;
+                for (int a = 0; a < pairLen; ++a) {
+                    if (PL[a][0] != k && PL[a][1] != k) continue;
+                    if (types[a] == 0) cont = 1;
+                    if (types[a] == 3 || types[a] == 4) accr = 1;
+                }
+                const float coef = cont ? ks->frictionCoefficientContinental
+                                        : (accr ? ks->frictionCoefficientAccretion : ks->frictionCoefficientSubduction);
+                const float massDiff = heights[k] / dyn[ids[k]].mass;
+                const float f = (plates[ids[k]].velocity * coef) * massDiff;
+                fric[ids[k]] += tecto_fix(f, OR_FRIC_SCALE, OR_FRIC_LIMIT);
+            }
         }
         int owner = 0;
         for (int i = 0; i < n; ++i)
@@ -986,9 +1024,139 @@ void or_ccl(int W, int H, const uint8_t *id, uint32_t *labels, int mode)
 /* ---- full step ---------------------------------------------------------------------------- */
 
 /* PlateTectonicSim::executeIteration (plate_tectonic_sim.cu:54-131), hot-path phases. */
+/* ---- plate dynamics ------------------------------------------------------------------------- */
+
+/* The per-plate values a step starts from: mass (sum of heights) and size over all cells, as
+ * mergeAndCountSizeMass leaves them without merges (plate_tectonics_kernel.cu:100-195), and the
+ * geometric centre of accumulatePlateAngularCoords / calculatePlateCenters (:2154-2226): the cells
+ * whose x and y are multiples of 10 contribute sin and cos of their angle around each axis, the
+ * means go back to a cell coordinate through atan2.  The sums are exact fixed-point sums (mass x 2^16,
+ * angular terms x 2^32).  Iteration 0 keeps the stored centre (the reference computes the first one
+ * at the end of its first iteration). */
+void or_plate_stats(int W, int H, const float *h, const uint8_t *id, uint32_t iteration,
+                    tecto_plate_dynamics *dyn)
+{
+    int64_t mass[NPLATE], ang[NPLATE][4];
+    int size[NPLATE], samples[NPLATE];
+    memset(mass, 0, sizeof(mass));
+    memset(ang, 0, sizeof(ang));
+    memset(size, 0, sizeof(size));
+    memset(samples, 0, sizeof(samples));
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const size_t d = (size_t)y * (size_t)W + (size_t)x;
+            const unsigned p = id[d];
+            if (p >= NPLATE) continue;
+            mass[p] += tecto_fix(h[d], OR_MASS_SCALE, OR_MASS_LIMIT);
+            size[p] += 1;
+            if (x % 10 == 0 && y % 10 == 0) {
+                const float ax = (OR_TWO_PI_F * (float)x) / (float)W;
+                const float ay = (OR_TWO_PI_F * (float)y) / (float)H;
+                ang[p][0] += tecto_fix(tecto_sinf(ax), OR_ANG_SCALE, 1.0f);
+                ang[p][1] += tecto_fix(tecto_cosf(ax), OR_ANG_SCALE, 1.0f);
+                ang[p][2] += tecto_fix(tecto_sinf(ay), OR_ANG_SCALE, 1.0f);
+                ang[p][3] += tecto_fix(tecto_cosf(ay), OR_ANG_SCALE, 1.0f);
+                samples[p] += 1;
+            }
+        }
+    for (unsigned p = 0; p < NPLATE; ++p) {
+        dyn[p].mass = tecto_unfix(mass[p], 1.0 / (double)OR_MASS_SCALE);
+        dyn[p].size = size[p];
+        if (samples[p] > 0 && iteration > 0) {
+            const float n = (float)samples[p];
+            const float sx = tecto_unfix(ang[p][0], 1.0 / (double)OR_ANG_SCALE) / n;
+            const float cx = tecto_unfix(ang[p][1], 1.0 / (double)OR_ANG_SCALE) / n;
+            const float sy = tecto_unfix(ang[p][2], 1.0 / (double)OR_ANG_SCALE) / n;
+            const float cy = tecto_unfix(ang[p][3], 1.0 / (double)OR_ANG_SCALE) / n;
+            float gx = tecto_atan2f(sx, cx) * (float)W / OR_TWO_PI_F;
+            float gy = tecto_atan2f(sy, cy) * (float)H / OR_TWO_PI_F;
+            if (gx < 0.0f) gx += (float)W;
+            if (gy < 0.0f) gy += (float)H;
+            dyn[p].geometricCenter_x = gx;
+            dyn[p].geometricCenter_y = gy;
+        }
+    }
+}
+
+static int wrap_i(int v, int n)
+{
+    const int r = v % n;
+    return r < 0 ? r + n : r;
+}
+
+/* computeCurl (plate_tectonics_kernel.cu:2788-2822) at world cell (cx, cy): the pressure texture
+ * (pw x ph) sampled nearest at (cx * pw / W, cy * ph / H), its central differences rotated. */
+void or_curl_at(const float *pr, int pw, int ph, int W, int H, int cx, int cy, float *out_x, float *out_y)
+{
+    const double xs = (double)pw / (double)W, ys = (double)ph / (double)H;
+    const int qx = (int)((double)cx * xs), qy = (int)((double)cy * ys);
+    const float left = pr[(size_t)qy * pw + wrap_i(qx - 1, pw)];
+    const float right = pr[(size_t)qy * pw + wrap_i(qx + 1, pw)];
+    const float bottom = pr[(size_t)wrap_i(qy - 1, ph) * pw + qx];
+    const float top = pr[(size_t)wrap_i(qy + 1, ph) * pw + qx];
+    *out_y = (float)((double)(right - left) * 0.5);
+    *out_x = (float)(-((double)(top - bottom) * 0.5));
+}
+
+/* applyPlateMovementChanges (plate_tectonics_kernel.cu:1863-1925) for velocity, direction,
+ * smoothing and the merge wait (the sub-cell centre update is or_plate_offsets'): the velocity
+ * loses the friction fric[k] (fixed point x 2^40), then drag pulls it towards the asthenosphere flow,
+ * the curl of the pressure texture at the plate's geometric centre (zero without a texture),
+ * offset by 0.2 away from zero and clamped to [-1, 1]. */
+void or_plate_motion(int W, int H, tecto_plate *plates, tecto_plate_dynamics *dyn, const int64_t *fric,
+                     const float *pressure, int pw, int ph, const tecto_kernel_settings *ks)
+{
+    for (unsigned k = 0; k < NPLATE; ++k) {
+        tecto_plate *p = &plates[k];
+        tecto_plate_dynamics *dd = &dyn[k];
+        const float friction = tecto_unfix(fric[k], 1.0 / (double)OR_FRIC_SCALE);
+        float sx = 0.0f, sy = 0.0f;
+        if (pressure) {
+            const float gx = fminf(fmaxf(dd->geometricCenter_x + 0.5f, -1073741824.0f), 1073741824.0f);
+            const float gy = fminf(fmaxf(dd->geometricCenter_y + 0.5f, -1073741824.0f), 1073741824.0f);
+            or_curl_at(pressure, pw, ph, W, H, wrap_i((int)gx, W), wrap_i((int)gy, H), &sx, &sy);
+        }
+        const float avx = fmaxf(fminf((float)((double)(sx * ks->curlNoiseMultiplier) + (sx < 0.0f ? -0.2 : 0.2)), 1.0f), -1.0f);
+        const float avy = fmaxf(fminf((float)((double)(sy * ks->curlNoiseMultiplier) + (sy < 0.0f ? -0.2 : 0.2)), 1.0f), -1.0f);
+        const float ox = p->direction_x * p->velocity, oy = p->direction_y * p->velocity;
+        const float mag = fmaxf(sqrtf(ox * ox + oy * oy), 1e-20f);
+        const float post = fmaxf(mag - friction, 0.0f);
+        const float vx = p->direction_x * post, vy = p->direction_y * post;
+        const float rx = avx - vx, ry = avy - vy;
+        const float rmag = sqrtf(rx * rx + ry * ry);
+        const float drag = ks->environmentalDragCoefficient * rmag * rmag;
+        const float rn = fmaxf(sqrtf(rx * rx + ry * ry), 1e-20f);
+        const float nx = vx + (rx / rn) * drag, ny = vy + (ry / rn) * drag;
+        const float nm = fmaxf(sqrtf(nx * nx + ny * ny), 1e-20f);
+        p->velocity = nm;
+        p->direction_x = nx / nm;
+        p->direction_y = ny / nm;
+        const float vs = ks->velocitySmoothingFactor, ds = ks->directionSmoothingFactor;
+        dd->velocitySmoothed = dd->velocitySmoothed * vs + p->velocity * (1.0f - vs);
+        const float sdx = dd->directionSmoothed_x * ds + p->direction_x * (1.0f - ds);
+        const float sdy = dd->directionSmoothed_y * ds + p->direction_y * (1.0f - ds);
+        const float sm = fmaxf(sqrtf(sdx * sdx + sdy * sdy), 1e-20f);
+        dd->directionSmoothed_x = sdx / sm;
+        dd->directionSmoothed_y = sdy / sm;
+        dd->mergeWaitTime = dd->mergeWaitTime > 0 ? dd->mergeWaitTime - 1 : 0;
+        dd->frictionLoss = friction;
+    }
+}
+
 void or_step(int W, int H, float *h, float *w, float *s, float *flux, uint8_t *id, uint32_t *labels,
              uint32_t *word, uint8_t *acc, uint8_t *bm, uint32_t *div_bitmap, tecto_plate *plates,
              const tecto_settings *st, uint32_t seed, uint32_t *iteration)
+{
+    or_step_dyn(W, H, h, w, s, flux, id, labels, word, acc, bm, div_bitmap, plates, NULL, NULL, 0, 0, st, seed,
+                iteration);
+}
+
+/* or_step with plate dynamics when st->step.plateDynamics is TECTO_PLATE_DYNAMICS_REFERENCE: dyn
+ * holds the plate dynamics records, pressure (pw x ph, or NULL) the asthenosphere texture. */
+void or_step_dyn(int W, int H, float *h, float *w, float *s, float *flux, uint8_t *id, uint32_t *labels,
+                 uint32_t *word, uint8_t *acc, uint8_t *bm, uint32_t *div_bitmap, tecto_plate *plates,
+                 tecto_plate_dynamics *dyn, const float *pressure, int pw, int ph, const tecto_settings *st,
+                 uint32_t seed, uint32_t *iteration)
 {
     const size_t N = (size_t)W * (size_t)H;
     int32_t offx[NPLATE], offy[NPLATE];
@@ -998,15 +1166,22 @@ void or_step(int W, int H, float *h, float *w, float *s, float *flux, uint8_t *i
     or_collision_types(W, H, word, h, offx, offy, &st->kernel, bm);
     float *hn = (float *)malloc(N * sizeof(float));
     uint8_t *idn = (uint8_t *)malloc(N);
+    const int dynamics = dyn && st->step.plateDynamics == TECTO_PLATE_DYNAMICS_REFERENCE;
+    int64_t fric[NPLATE];
+    memset(fric, 0, sizeof(fric));
+    if (dynamics) or_plate_stats(W, H, h, id, *iteration, dyn);
+    float *uh = NULL;
+    uint8_t *ut = NULL;
     if (st->step.upliftMode == TECTO_UPLIFT_REFERENCE) {
-        float *uh = (float *)calloc(N, sizeof(float));
-        uint8_t *ut = (uint8_t *)calloc(N, 1);
-        or_resolve_ex(W, H, id, h, word, offx, offy, bm, div_bitmap, st, seed, *iteration, hn, idn, acc, uh, ut);
+        uh = (float *)calloc(N, sizeof(float));
+        ut = (uint8_t *)calloc(N, 1);
+    }
+    or_resolve_dyn(W, H, id, h, word, offx, offy, bm, div_bitmap, st, seed, *iteration, hn, idn, acc, uh, ut,
+                   plates, dyn, dynamics ? fric : NULL);
+    if (st->step.upliftMode == TECTO_UPLIFT_REFERENCE) {
         or_uplift_ref(W, H, word, uh, ut, h, plates, idn, hn, &st->kernel, NULL, NULL);
         free(uh);
         free(ut);
-    } else {
-        or_resolve(W, H, id, h, word, offx, offy, bm, div_bitmap, st, seed, *iteration, hn, idn, acc);
     }
     memcpy(h, hn, N * sizeof(float));
     memcpy(id, idn, N);
@@ -1015,8 +1190,9 @@ void or_step(int W, int H, float *h, float *w, float *s, float *flux, uint8_t *i
     or_thermal(W, H, h, st->step.thermalIterations, &st->kernel);
     or_hydraulic(W, H, h, w, s, flux, st->step.hydraulicIterations, st->step.hydraulicDt,
                  seed + *iteration, &st->kernel);
-    or_accretion(W, H, h, acc, id, &st->kernel);
     memcpy(plates, next, sizeof(next));
+    if (dynamics) or_plate_motion(W, H, plates, dyn, fric, pressure, pw, ph, &st->kernel);
+    or_accretion(W, H, h, acc, id, &st->kernel);
     const int period = st->sim.iterationsForCCL > 0 ? st->sim.iterationsForCCL : 1;
     if (*iteration % (uint32_t)period == 0) or_ccl(W, H, id, labels, st->step.cclConnectivity);
     *iteration += 1;

@@ -82,6 +82,25 @@ void or_step(int W, int H, float *h, float *w, float *s, float *flux, uint8_t *i
              uint32_t *div_bitmap, tecto_plate *plates, const tecto_settings *st, uint32_t seed,
              uint32_t *iteration);
 
+/* processCollisions with plate dynamics' friction per plate (fixed point x 2^40 in fric[255]; plates:
+ * velocities, dyn: masses); or_resolve_ex when fric is NULL. */
+void or_resolve_dyn(int W, int H, const uint8_t *id_old, const float *h_old, const uint32_t *word,
+                    const int32_t *off_x, const int32_t *off_y, const uint8_t *bm, uint32_t *div_bitmap,
+                    const tecto_settings *st, uint32_t seed, uint32_t iteration, float *h_new,
+                    uint8_t *id_new, uint8_t *acc, float *up_h, uint8_t *up_t, const tecto_plate *plates,
+                    const tecto_plate_dynamics *dyn, int64_t *fric);
+/* Plate dynamics: per-plate mass, size and geometric centre of a state; computeCurl at one cell;
+ * applyPlateMovementChanges; a whole step with dynamics (dyn NULL or plateDynamics off: or_step). */
+void or_plate_stats(int W, int H, const float *h, const uint8_t *id, uint32_t iteration,
+                    tecto_plate_dynamics *dyn);
+void or_curl_at(const float *pr, int pw, int ph, int W, int H, int cx, int cy, float *out_x, float *out_y);
+void or_plate_motion(int W, int H, tecto_plate *plates, tecto_plate_dynamics *dyn, const int64_t *fric,
+                     const float *pressure, int pw, int ph, const tecto_kernel_settings *ks);
+void or_step_dyn(int W, int H, float *h, float *w, float *s, float *flux, uint8_t *id, uint32_t *labels,
+                 uint32_t *word, uint8_t *acc, uint8_t *bm, uint32_t *div_bitmap, tecto_plate *plates,
+                 tecto_plate_dynamics *dyn, const float *pressure, int pw, int ph, const tecto_settings *st,
+                 uint32_t seed, uint32_t *iteration);
+
 /* Image export (src/cuda_compute/texture_save.cu): convertFloatToGray16Kernel (:80-96) over n
  * heights, and convertGrayscaleToRgbKernel's colour (:16-70) of every plate id as a 256 x 3 palette. */
 void or_gray16(size_t n, const float *h, float minv, float maxv, uint16_t *out);

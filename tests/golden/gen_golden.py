@@ -226,6 +226,68 @@ def ref_export(name):
     print("wrote", name)
 
 
+def ref_dynamics(name):
+    """Plate dynamics kernels of the reference: processCollisions' friction per plate on an evolved
+    world, the angular geometric centres, computeCurl of a pressure texture and
+    applyPlateMovementChanges on given plate records."""
+    R = O.ref()
+    W, H = 64, 64
+    st = T.baseline_settings()
+    st.kernel.minCollisionSize = 3
+    st.kernel.collisionTypeUpdateCooldown = 2
+    st.kernel.frictionCoefficientContinental = 0.3
+    st.kernel.frictionCoefficientSubduction = 0.05
+    st.kernel.frictionCoefficientAccretion = 0.15
+    R.ref_set_settings(C.addressof(st.kernel))
+    h, ids, pl = T.generate_world(W, H, 7, 1.5, 23)
+    ow = O.OracleWorld(st, h, ids, pl, 1000)
+    ow.step(3)
+    # the collide phases of the next step, from the oracle (pinned by the step compositions)
+    offx, offy, _ = O.plate_offsets(ow.plates)
+    _, word, _, _ = O.collision_words(ow.id, offx, offy)
+    bitmap = O.collision_types(word, ow.h, offx, offy, st, ow.bitmap)
+    dyn = O.plate_stats(ow.h, ow.id, 3)
+    mass = np.ascontiguousarray(dyn["mass"], np.float32)
+    fric = np.zeros(255, np.float32)
+    R.ref_collision_friction(W, H, P(ow.id), P(ow.h), P(word), P(ow.plates), P(mass), P(bitmap), P(ow.div), 1000, 3,
+                             P(fric))
+    # centres: the evolved ids, and a map with plates across both seams
+    centres = np.zeros((255, 2), np.float32)
+    R.ref_plate_centres(W, H, P(ow.id), P(centres))
+    ids2 = np.full((50, 70), 3, np.uint8)  # plates 1 and 2 straddle the seams; 3 is the background
+    ids2[:30, :12] = 1
+    ids2[:30, 61:] = 1
+    ids2[:8, 20:40] = 2
+    ids2[44:, 20:40] = 2
+    centres2 = np.zeros((255, 2), np.float32)
+    R.ref_plate_centres(70, 50, P(ids2), P(centres2))
+    # curl of a random pressure texture, nearest-scaled from 40 x 28 to 64 x 64
+    rng = np.random.default_rng(29)
+    pressure = rng.random((28, 40)).astype(np.float32)
+    curl = np.zeros((H, W, 2), np.float32)
+    R.ref_curl(40, 28, P(pressure), W, H, P(curl))
+    # movement changes on synthetic records
+    plates_in = ow.plates.copy()
+    dyn_in = np.zeros(255, T.PLATE_DYNAMICS_DTYPE)
+    dyn_in["velocitySmoothed"] = rng.uniform(0.0, 1.0, 255)
+    ang = rng.uniform(0.0, 2 * np.pi, 255)
+    dyn_in["directionSmoothed_x"] = np.cos(ang)
+    dyn_in["directionSmoothed_y"] = np.sin(ang)
+    dyn_in["geometricCenter_x"] = rng.uniform(0.0, W, 255)
+    dyn_in["geometricCenter_y"] = rng.uniform(0.0, H, 255)
+    dyn_in["mergeWaitTime"] = rng.integers(0, 3, 255)
+    fric_in = rng.uniform(0.0, 0.5, 255).astype(np.float32)
+    fric_in[:20] = 0.0
+    plates_out, dyn_out = plates_in.copy(), dyn_in.copy()
+    R.ref_plate_motion(W, H, P(plates_out), P(dyn_out), P(fric_in), P(curl))
+    np.savez_compressed(OUT / f"{name}.npz", W=W, H=H, ids=ow.id, h=ow.h, word=word, plates=ow.plates,
+                        bitmap=bitmap, div=ow.div, mass=mass, friction=fric, centres=centres, ids2=ids2,
+                        centres2=centres2, pressure=pressure, curl=curl, plates_in=plates_in, dyn_in=dyn_in,
+                        fric_in=fric_in, plates_out=plates_out, dyn_out=dyn_out,
+                        fc=np.float32([0.3, 0.05, 0.15]))
+    print("wrote", name, "plates with friction", int((fric != 0).sum()))
+
+
 def main():
     O.build(ref=True)
     ref_step_composition("ref_steps_baseline_64x64", 64, 64, 8, 1.0, 7, "baseline", 6, 20, 0.02)
@@ -235,6 +297,7 @@ def main():
     ref_thermal_isolated("ref_thermal_isolated_64x64", 64, 64, 13)
     ref_ccl_cases("ref_ccl_cases")
     ref_export("ref_export")
+    ref_dynamics("ref_dynamics")
 
 
 if __name__ == "__main__":
