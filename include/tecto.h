@@ -458,6 +458,21 @@ int tecto_server_set_output(tecto_server *server, const char *directory, int wha
 /* Dry-run cost model: seconds one tick takes per million active cells (default 2e-4). */
 int tecto_server_set_dry_cost(tecto_server *server, double seconds_per_mcell_step);
 
+/* The reference's world initialisation (PlateTectonicSim::initializeTectonics,
+ * plate_tectonic_sim.cu:705-773) from the world's settings (sim.numStartingPlates,
+ * sim.numVoronoiSeeds[0..numVoronoiGenerations)) and its seed: plate centres, Voronoi seed
+ * generations and plate kinematics drawn on the host from std::default_random_engine through
+ * std::uniform_real_distribution<float> in the reference's order; the nearest-seed plate ids
+ * (initPlateIDs) and the simplex height map (initHeightmap, 5000..15000) on the device; CCL labels.
+ * Everything else starts at zero, iteration 0.  Plate fragments keep their id (the reference's
+ * post-CCL relabel is not part of this engine). */
+int tecto_world_init_reference(tecto_world *world, tecto_stream_t stream);
+/* The host part alone: seed_x / seed_y / seed_id (capacity entries; *count = seeds of the last
+ * generation, or the plate centres) and the plate records it draws. */
+int tecto_reference_seeds(int width, int height, uint32_t seed, int numPlates, const int *numVoronoiSeeds,
+                          int generations, float *seed_x, float *seed_y, uint8_t *seed_id, int capacity,
+                          int *count, tecto_plate *plates, tecto_plate_dynamics *dynamics);
+
 /* Device-side synthetic generator: same result as tecto_generate_world_host, computed on the GPU
  * (the on-device world init the server uses). */
 int tecto_world_init_synthetic_device(tecto_world *world, int numPlates, float velRange,

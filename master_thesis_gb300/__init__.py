@@ -252,6 +252,9 @@ def _declare(L: C.CDLL) -> None:
         "tecto_world_launch_count": ([P, C.POINTER(C.c_uint64)], C.c_int),
         "tecto_world_bytes": ([C.c_int, C.c_int], C.c_size_t),
         "tecto_world_init_synthetic_device": ([P, C.c_int, C.c_float, C.c_uint64, P], C.c_int),
+        "tecto_world_init_reference": ([P, P], C.c_int),
+        "tecto_reference_seeds": ([C.c_int, C.c_int, C.c_uint32, C.c_int, P, C.c_int, P, P, P, C.c_int,
+                                   C.POINTER(C.c_int), P, P], C.c_int),
         "tecto_batch_create": ([C.POINTER(P)], C.c_int),
         "tecto_batch_destroy": ([P], C.c_int),
         "tecto_batch_add": ([P, P, P], C.c_int),
@@ -543,6 +546,31 @@ def _world_init_device(self, plates: int, vel_range: float, gen_seed: int, strea
 
 
 World.init_synthetic_device = _world_init_device
+
+
+def _world_init_reference(self, stream=None) -> None:
+    """The reference's initialisation (initializeTectonics) from the world's settings and seed."""
+    check(lib().tecto_world_init_reference(self.ptr, _stream(stream)), "tecto_world_init_reference")
+
+
+World.init_reference = _world_init_reference
+
+
+def reference_seeds(W: int, H: int, seed: int, num_plates: int, gens):
+    """The host draws of the reference's initialisation: (seed x, seed y, seed plate id, plates,
+    plate dynamics records)."""
+    g = np.ascontiguousarray(gens, np.int32)
+    cap = max([num_plates] + [int(v) for v in g])
+    sx, sy = np.zeros(cap, np.float32), np.zeros(cap, np.float32)
+    sid = np.zeros(cap, np.uint8)
+    n = C.c_int(0)
+    pl = np.zeros(MAX_PLATES, PLATE_DTYPE)
+    dy = np.zeros(MAX_PLATES, PLATE_DYNAMICS_DTYPE)
+    check(lib().tecto_reference_seeds(W, H, seed, num_plates, g.ctypes.data if len(g) else None, len(g),
+                                      sx.ctypes.data, sy.ctypes.data, sid.ctypes.data, cap, C.byref(n),
+                                      pl.ctypes.data, dy.ctypes.data), "tecto_reference_seeds")
+    k = n.value
+    return sx[:k].copy(), sy[:k].copy(), sid[:k].copy(), pl, dy
 
 
 def world_bytes(W: int, H: int) -> int:

@@ -31,6 +31,7 @@ SOURCES = [
     "k_erosion.cu",
     "k_ccl.cu",
     "tecto_export.cu",
+    "tecto_init.cu",
     "settings.cpp",
 ]
 

@@ -126,6 +126,8 @@ def lib() -> C.CDLL:
         L.or_plate_stats.argtypes = [C.c_int, C.c_int, V, V, C.c_uint32, V]
         L.or_curl_at.argtypes = [V, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, V, V]
         L.or_plate_motion.argtypes = [C.c_int, C.c_int, V, V, V, V, C.c_int, C.c_int, V]
+        L.or_reference_seeds.argtypes = [C.c_int, C.c_int, C.c_uint32, C.c_int, V, C.c_int, V, V, V, C.c_int, V, V, V]
+        L.or_init_reference.argtypes = [C.c_int, C.c_int, C.c_uint32, V, V, V, C.c_int, V, V]
         L.or_hash.argtypes = [C.c_uint32]
         L.or_hash.restype = C.c_uint32
         L.or_simplex3.argtypes = [C.c_float] * 4 + [C.c_int]
@@ -173,6 +175,7 @@ def ref() -> C.CDLL:
         L.ref_plate_centres.argtypes = [C.c_int, C.c_int, V, V]
         L.ref_curl.argtypes = [C.c_int, C.c_int, V, C.c_int, C.c_int, V]
         L.ref_plate_motion.argtypes = [C.c_int, C.c_int, V, V, V, V]
+        L.ref_init.argtypes = [C.c_int, C.c_int, C.c_int, V, V, V, C.c_int, V, V]
         L.ref_ids_rgb.argtypes = [C.c_int, C.c_int, V, V]
         _r = L
     return _r
@@ -248,6 +251,32 @@ def expf(x: float) -> float:
 
 def log10f(x: float) -> float:
     return lib().or_log10f(x)
+
+
+def reference_seeds(W, H, seed, num_plates, gens):
+    """or_reference_seeds: (x, y, id) of the seeds, plate records, plate dynamics records."""
+    from master_thesis_gb300 import MAX_PLATES, PLATE_DTYPE, PLATE_DYNAMICS_DTYPE
+    g = np.ascontiguousarray(gens, np.int32)
+    cap = max([num_plates] + [int(v) for v in g])
+    sx, sy = np.zeros(cap, np.float32), np.zeros(cap, np.float32)
+    sid = np.zeros(cap, np.uint8)
+    n = C.c_int(0)
+    pl = np.zeros(MAX_PLATES, PLATE_DTYPE)
+    dy = np.zeros(MAX_PLATES, PLATE_DYNAMICS_DTYPE)
+    if lib().or_reference_seeds(W, H, seed, num_plates, _P(g), len(g), _P(sx), _P(sy), _P(sid), cap, C.byref(n),
+                                _P(pl), _P(dy)) != 0:
+        raise ValueError("invalid reference seed settings")
+    k = n.value
+    return sx[:k].copy(), sy[:k].copy(), sid[:k].copy(), pl, dy
+
+
+def init_reference(W, H, seed, sx, sy, sid):
+    """or_init_reference: (heights f32[H, W], plate ids u8[H, W])."""
+    h = np.zeros((H, W), np.float32)
+    ids = np.zeros((H, W), np.uint8)
+    sx, sy, sid = (np.ascontiguousarray(a, t) for a, t in ((sx, np.float32), (sy, np.float32), (sid, np.uint8)))
+    lib().or_init_reference(W, H, seed, _P(sx), _P(sy), _P(sid), len(sx), _P(h), _P(ids))
+    return h, ids
 
 
 def plate_stats(h, ids, iteration, dyn=None):

@@ -396,4 +396,19 @@ void ref_plate_motion(int W, int H, tecto_plate *plates, tecto_plate_dynamics *d
     }
 }
 
+/* initPlateIDs + initHeightmap (plate_tectonics_kernel.cu:31-99) for the given seeds. */
+void ref_init(int W, int H, int seed, const float *sx, const float *sy, const uint8_t *sid, int S, float *h,
+              uint8_t *id)
+{
+    std::vector<VoronoiSeed> seeds((size_t)S);
+    for (int k = 0; k < S; ++k) {
+        seeds[(size_t)k].position = Vec2<float>(sx[k], sy[k]);
+        seeds[(size_t)k].id = sid[k];
+    }
+    CudaTexture<uint8_t> tId(id, Vec2<int>(W, H));
+    CudaTexture<float> tH(h, Vec2<int>(W, H));
+    launch(blocks_for((size_t)W * H), TPB, [&] { initPlateIDs(&tId, seeds.data(), S); });
+    launch(blocks_for((size_t)W * H), TPB, [&] { initHeightmap(&tH, seed, 4); });
+}
+
 } // extern "C"

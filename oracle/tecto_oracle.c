@@ -1243,3 +1243,165 @@ void or_plate_palette(uint8_t *rgb768)
         o[2] = (uint8_t)lroundf((b + m) * 255.0f);
     }
 }
+
+/* ---- the reference's world initialisation ---------------------------------------------------- */
+
+/* std::default_random_engine as libstdc++ defines it (minstd_rand0: x <- 16807 x mod 2^31 - 1, a seed
+ * that is 0 mod the modulus becomes 1) and std::uniform_real_distribution<float> on it: one draw of
+ * generate_canonical<float, 24> (the engine spans 31 bits, so a single call: (x - 1) / (float)(2^31 - 2),
+ * the divisor rounding to 2^31, results of 1 pulled below 1), scaled to [a, b) as u * (b - a) + a. */
+typedef struct {
+    uint64_t x;
+} or_minstd;
+
+static void minstd_seed(or_minstd *g, uint64_t s)
+{
+    const uint64_t r = s % 2147483647u;
+    g->x = r == 0 ? 1u : r;
+}
+
+static float minstd_uniform(or_minstd *g, float a, float b)
+{
+    g->x = (g->x * 16807u) % 2147483647u;
+    const float sum = (float)(g->x - 1u) * 1.0f;
+    float u = sum / 2147483648.0f;
+    if (u >= 1.0f) u = nextafterf(1.0f, 0.0f);
+    return (u * (b - a)) + a;
+}
+
+/* PlateTectonicSim::initializeTectonics' host part (plate_tectonic_sim.cu:705-745):
+ * generatePlateCenters (:873-890), the generations of generateVoronoiSeeds (:892-929) and
+ * generatePlateData (:816-842).  Positions are drawn as {height range, width range}, as the
+ * reference does.  Returns 0, or -1 for invalid arguments or too small a capacity. */
+int or_reference_seeds(int W, int H, uint32_t seed, int numPlates, const int *gens, int ngens, float *seed_x,
+                       float *seed_y, uint8_t *seed_id, int capacity, int *count, tecto_plate *plates,
+                       tecto_plate_dynamics *dyn)
+{
+    if (numPlates < 1 || numPlates > (int)NPLATE || ngens < 0 || ngens > TECTO_MAX_VORONOI_GENS) return -1;
+    int maxn = numPlates;
+    for (int g = 0; g < ngens; ++g) {
+        if (gens[g] < 0 || gens[g] > (1 << 20)) return -1;
+        if (gens[g] > maxn) maxn = gens[g];
+    }
+    or_minstd rng;
+    minstd_seed(&rng, seed);
+    float *cx = (float *)malloc(sizeof(float) * (size_t)numPlates), *cy = (float *)malloc(sizeof(float) * (size_t)numPlates);
+    float *px = (float *)malloc(sizeof(float) * (size_t)maxn), *py = (float *)malloc(sizeof(float) * (size_t)maxn);
+    float *nx = (float *)malloc(sizeof(float) * (size_t)maxn), *ny = (float *)malloc(sizeof(float) * (size_t)maxn);
+    int *pid = (int *)malloc(sizeof(int) * (size_t)maxn), *nid = (int *)malloc(sizeof(int) * (size_t)maxn);
+    for (int i = 0; i < numPlates; ++i) {
+        cx[i] = minstd_uniform(&rng, 0.0f, (float)H);
+        cy[i] = minstd_uniform(&rng, 0.0f, (float)W);
+        px[i] = cx[i];
+        py[i] = cy[i];
+        pid[i] = i;
+    }
+    int n = numPlates;
+    for (int g = 0; g < ngens; ++g) {
+        for (int i = 0; i < gens[g]; ++i) {
+            const float sx = minstd_uniform(&rng, 0.0f, (float)H);
+            const float sy = minstd_uniform(&rng, 0.0f, (float)W);
+            float best = 3.40282347e38f;
+            int id = 0;
+            for (int c = 0; c < n; ++c) {
+                const float dx = fabsf(sx - px[c]), dy = fabsf(sy - py[c]);
+                const float wx = fminf(dx, (float)W - dx), wy = fminf(dy, (float)H - dy);
+                const float d2 = wx * wx + wy * wy;
+                if (d2 < best) {
+                    id = pid[c];
+                    best = d2;
+                }
+            }
+            nx[i] = sx;
+            ny[i] = sy;
+            nid[i] = id;
+        }
+        n = gens[g];
+        memcpy(px, nx, sizeof(float) * (size_t)n);
+        memcpy(py, ny, sizeof(float) * (size_t)n);
+        memcpy(pid, nid, sizeof(int) * (size_t)n);
+    }
+    if (n < numPlates) {
+        n = numPlates;
+        for (int i = 0; i < n; ++i) {
+            px[i] = cx[i];
+            py[i] = cy[i];
+            pid[i] = i;
+        }
+    }
+    int rc = 0;
+    *count = n;
+    if (seed_x || seed_y || seed_id) {
+        if (capacity < n) rc = -1;
+        else
+            for (int i = 0; i < n; ++i) {
+                if (seed_x) seed_x[i] = px[i];
+                if (seed_y) seed_y[i] = py[i];
+                if (seed_id) seed_id[i] = (uint8_t)pid[i];
+            }
+    }
+    if (plates) memset(plates, 0, sizeof(tecto_plate) * NPLATE);
+    if (dyn) memset(dyn, 0, sizeof(tecto_plate_dynamics) * NPLATE);
+    for (int i = 0; i < numPlates; ++i) {
+        const float v = (minstd_uniform(&rng, -1.0f, 1.0f) + 1.0f) / 2.0f;
+        const float xd = minstd_uniform(&rng, -1.0f, 1.0f);
+        const float yd = minstd_uniform(&rng, -1.0f, 1.0f);
+        const float m = sqrtf(xd * xd + yd * yd);
+        if (plates) {
+            plates[i].pixelCenter_x = cx[i] - floorf(cx[i]);
+            plates[i].pixelCenter_y = cy[i] - floorf(cy[i]);
+            plates[i].velocity = v;
+            plates[i].direction_x = xd / m;
+            plates[i].direction_y = yd / m;
+        }
+        if (dyn) {
+            dyn[i].velocitySmoothed = v;
+            dyn[i].directionSmoothed_x = xd / m;
+            dyn[i].directionSmoothed_y = yd / m;
+        }
+    }
+    free(cx); free(cy); free(px); free(py); free(nx); free(ny); free(pid); free(nid);
+    return rc;
+}
+
+/* initPlateIDs (plate_tectonics_kernel.cu:31-63): the first seed at the minimum wrapped squared
+ * distance; initHeightmap (:65-99): four octaves of simplex noise at frequencies 0.01 x 10^k with
+ * amplitudes 0.9 x 0.1^k, each remapped from [-1, 1] to [0, 1] after damping by 1 + |gradient|
+ * (forward differences at 0.001 cells), scaled to 5000..15000. */
+void or_init_reference(int W, int H, uint32_t seed, const float *sx, const float *sy, const uint8_t *sid, int S,
+                       float *h, uint8_t *id)
+{
+#pragma omp parallel for schedule(static)
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const size_t i = (size_t)y * (size_t)W + (size_t)x;
+            const float fx = (float)x, fy = (float)y;
+            float best = 3.40282347e38f;
+            int plate = 0;
+            for (int k = 0; k < S; ++k) {
+                const float dx = fabsf(fx - sx[k]), dy = fabsf(fy - sy[k]);
+                const float wx = fminf(dx, (float)W - dx), wy = fminf(dy, (float)H - dy);
+                const float d2 = wx * wx + wy * wy;
+                if (d2 < best) {
+                    plate = sid[k];
+                    best = d2;
+                }
+            }
+            id[i] = (uint8_t)plate;
+            const float d = 0.001f;
+            float value = 0.0f, amp = 0.9f, freq = 0.01f;
+            for (int octave = 0; octave < 4; ++octave) {
+                const int sd = (int)seed + octave;
+                const float v = or_simplex3(fx, fy, 0.0f, freq, sd);
+                const float vx = or_simplex3(fx + d, fy, 0.0f, freq, sd);
+                const float vy = or_simplex3(fx, fy + d, 0.0f, freq, sd);
+                const float gx = (vx - v) / d, gy = (vy - v) / d;
+                const float mag = sqrtf(gx * gx + gy * gy);
+                const float r = 0.0f + 1.0f * ((v / (1.0f + mag) - -1.0f) / (1.0f - -1.0f));
+                value = value + r * amp;
+                amp = amp * 0.1f;
+                freq = freq * 10.0f;
+            }
+            h[i] = 5000.0f + value * (15000.0f - 5000.0f);
+        }
+}

@@ -106,6 +106,14 @@ void or_step_dyn(int W, int H, float *h, float *w, float *s, float *flux, uint8_
 void or_gray16(size_t n, const float *h, float minv, float maxv, uint16_t *out);
 void or_plate_palette(uint8_t *rgb768);
 
+/* The reference's world initialisation: the host draws (seeds of the last Voronoi generation, plate
+ * records) and the per-cell plate ids and height map. */
+int or_reference_seeds(int W, int H, uint32_t seed, int numPlates, const int *gens, int ngens, float *seed_x,
+                       float *seed_y, uint8_t *seed_id, int capacity, int *count, tecto_plate *plates,
+                       tecto_plate_dynamics *dyn);
+void or_init_reference(int W, int H, uint32_t seed, const float *sx, const float *sy, const uint8_t *sid, int S,
+                       float *h, uint8_t *id);
+
 /* Building blocks exposed for unit tests. */
 uint32_t or_hash(uint32_t v);
 float or_simplex3(float x, float y, float z, float scale, int seed);

@@ -288,6 +288,23 @@ def ref_dynamics(name):
     print("wrote", name, "plates with friction", int((fric != 0).sum()))
 
 
+def ref_init(name):
+    """The reference's initPlateIDs and initHeightmap for seeds of the reference's draws (two
+    Voronoi generations, a non-square world, so the swapped position ranges show)."""
+    R = O.ref()
+    out = {}
+    for tag, (W, H, seed, plates, gens) in {"a": (96, 64, 1234, 12, (60, 150)), "b": (50, 80, 7, 5, ())}.items():
+        sx, sy, sid, pl, dy = O.reference_seeds(W, H, seed, plates, gens)
+        h = np.zeros((H, W), np.float32)
+        ids = np.zeros((H, W), np.uint8)
+        R.ref_init(W, H, seed, P(sx), P(sy), P(sid), len(sx), P(h), P(ids))
+        out.update({f"{tag}_W": W, f"{tag}_H": H, f"{tag}_seed": seed, f"{tag}_plates": plates,
+                    f"{tag}_gens": np.array(gens, np.int32), f"{tag}_sx": sx, f"{tag}_sy": sy, f"{tag}_sid": sid,
+                    f"{tag}_h": h, f"{tag}_ids": ids})
+    np.savez_compressed(OUT / f"{name}.npz", **out)
+    print("wrote", name)
+
+
 def main():
     O.build(ref=True)
     ref_step_composition("ref_steps_baseline_64x64", 64, 64, 8, 1.0, 7, "baseline", 6, 20, 0.02)
@@ -298,6 +315,7 @@ def main():
     ref_ccl_cases("ref_ccl_cases")
     ref_export("ref_export")
     ref_dynamics("ref_dynamics")
+    ref_init("ref_init")
 
 
 if __name__ == "__main__":

@@ -1,0 +1,67 @@
+"""The reference's world initialisation on the GPU (tecto_world_init_reference) against the oracle,
+which the reference's own kernels pin (test_oracle_init.py): plate ids, heights, plate records and
+CCL labels bit for bit, and the first steps of the initialised world."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import master_thesis_gb300 as T
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def stream():
+    torch = pytest.importorskip("torch")
+    assert torch.cuda.is_available(), "a CUDA GPU is required"
+    return torch.cuda.Stream()
+
+
+def settings(plates, gens):
+    s = T.default_settings()
+    s.step.upliftMode = T.UPLIFT_GAUSSIAN
+    s.kernel.minCollisionSize = 3
+    s.kernel.collisionTypeUpdateCooldown = 2
+    s.sim.iterationsForCCL = 3
+    s.sim.numStartingPlates = plates
+    s.sim.numVoronoiGenerations = len(gens)
+    for i, v in enumerate(gens):
+        s.sim.numVoronoiSeeds[i] = v
+    return s
+
+
+@pytest.mark.parametrize("W,H,seed,plates,gens", [(96, 64, 1234, 12, (60, 150)), (50, 80, 7, 5, ()),
+                                                  (512, 384, 42, 16, (200, 500)), (300, 200, 5, 30, (3000,))])
+def test_init_matches_oracle(stream, W, H, seed, plates, gens):
+    s = settings(plates, gens)
+    w = T.World(s, W, H, seed=seed)
+    w.init_reference(stream)
+    sx, sy, sid, pl, dy = O.reference_seeds(W, H, seed, plates, gens)
+    h, ids = O.init_reference(W, H, seed, sx, sy, sid)
+    np.testing.assert_array_equal(w.download(T.FIELD_PLATE_ID, stream), ids)
+    np.testing.assert_array_equal(w.download(T.FIELD_HEIGHT, stream), h)
+    np.testing.assert_array_equal(w.plates(stream), pl)
+    got = w.plate_dynamics(stream)
+    for f in ("velocitySmoothed", "directionSmoothed_x", "directionSmoothed_y"):
+        np.testing.assert_array_equal(got[f], dy[f])
+    labels = np.zeros((H, W), np.uint32)
+    O.lib().or_ccl(W, H, O._P(ids), O._P(labels), s.step.cclConnectivity)
+    np.testing.assert_array_equal(w.download(T.FIELD_LABELS, stream), labels)
+    assert w.iteration == 0
+    assert not w.download(T.FIELD_WATER, stream).any()
+
+
+def test_initialised_world_steps_like_the_oracle(stream):
+    W, H, seed = 128, 96, 77
+    s = settings(10, (80,))
+    w = T.World(s, W, H, seed=seed)
+    w.init_reference(stream)
+    o = O.OracleWorld(s, w.download(T.FIELD_HEIGHT, stream), w.download(T.FIELD_PLATE_ID, stream), w.plates(stream),
+                      seed)
+    for step in range(4):
+        w.step(1, stream)
+        o.step(1)
+        np.testing.assert_array_equal(w.download(T.FIELD_PLATE_ID, stream), o.id, err_msg=f"ids step {step}")
+        np.testing.assert_array_equal(w.download(T.FIELD_HEIGHT, stream), o.h, err_msg=f"heights step {step}")
