@@ -490,6 +490,41 @@ def engine_extras(args, T, torch, stream, s, specs, total, batched_value):
                          "step_roofline_frac": (STEP_BYTES_PER_CELL + 4.5) * v8192 / 1e9 / peak}
     torch.cuda.empty_cache()
 
+    # the widened rows: plate dynamics' cost per step, the reference's initialisation, the exports
+    sd = T.baseline_settings()
+    sd.step.plateDynamics = T.PLATE_DYNAMICS_REFERENCE
+    _, msd = plain_world_rate(T, torch, stream, 2048, 2048, 32, 1.0, 20, sd)
+    out["plate_dynamics_2048"] = {"ms_per_step": msd, "ms_per_step_without": ms2048,
+                                  "overhead_frac": msd / ms2048 - 1.0,
+                                  "workload": "one 2048x2048 world, 32 plates, plate dynamics on"}
+    si = T.default_settings()  # the reference's defaults: 16 plates, Voronoi generations of 200 and 500 seeds
+    w = T.World(si, 2048, 2048, seed=1000)
+    w.init_reference(stream)
+    init_ms = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        w.init_reference(stream)
+        stream.synchronize()
+        init_ms.append((time.perf_counter() - t0) * 1e3)
+    import tempfile
+    exp_ms = {}
+    with tempfile.TemporaryDirectory() as d:
+        for name, kind in (("height_gray16", T.EXPORT_HEIGHT_GRAY16), ("plates_rgb", T.EXPORT_PLATES_RGB)):
+            t0 = time.perf_counter()
+            w.export_png(kind, os.path.join(d, name + ".png"), si.kernel.minUpliftClamp, si.kernel.maxUpliftClamp,
+                         stream)
+            exp_ms[name] = (time.perf_counter() - t0) * 1e3
+        t0 = time.perf_counter()
+        w.save_snapshot(os.path.join(d, "w.snap"), stream)
+        exp_ms["snapshot_save"] = (time.perf_counter() - t0) * 1e3
+        t0 = time.perf_counter()
+        w.load_snapshot(os.path.join(d, "w.snap"), stream)
+        exp_ms["snapshot_load"] = (time.perf_counter() - t0) * 1e3
+    w.close()
+    out["init_reference_2048"] = {"ms": min(init_ms), "workload": "2048x2048, the reference's default settings "
+                                  "(16 plates, Voronoi generations of 200 and 500 seeds), wall time incl. host draws"}
+    out["output_2048_ms"] = exp_ms
+
     # serving: plain-path service time per request size sets the arrival rate
     svc = {}
     for side in (256, 1024, 4096):

@@ -455,6 +455,13 @@ int tecto_server_run_trace_sequential(tecto_server *server, const tecto_request 
 #define TECTO_SERVER_OUT_SNAPSHOT 4
 int tecto_server_set_output(tecto_server *server, const char *directory, int what, float height_min,
                             float height_max);
+/* How admitted worlds are initialised on the device: TECTO_SERVER_INIT_SYNTHETIC (default: the
+ * engine's generator with the request's plates, velRange and genSeed) or TECTO_SERVER_INIT_REFERENCE
+ * (tecto_world_init_reference with numStartingPlates = the request's plates, the server settings'
+ * Voronoi generations and the request's worldSeed). */
+#define TECTO_SERVER_INIT_SYNTHETIC 0
+#define TECTO_SERVER_INIT_REFERENCE 1
+int tecto_server_set_init(tecto_server *server, int mode);
 /* Dry-run cost model: seconds one tick takes per million active cells (default 2e-4). */
 int tecto_server_set_dry_cost(tecto_server *server, double seconds_per_mcell_step);
 

@@ -37,6 +37,7 @@ PLATE_DYNAMICS_OFF, PLATE_DYNAMICS_REFERENCE = 0, 1
 PNG_GRAY16, PNG_RGB8, PNG_GRAY8 = 0, 1, 2
 EXPORT_HEIGHT_GRAY16, EXPORT_PLATES_RGB = 0, 1
 SERVER_OUT_HEIGHT_PNG, SERVER_OUT_PLATES_PNG, SERVER_OUT_SNAPSHOT = 1, 2, 4
+SERVER_INIT_SYNTHETIC, SERVER_INIT_REFERENCE = 0, 1
 
 (FIELD_HEIGHT, FIELD_WATER, FIELD_SEDIMENT, FIELD_FLUX, FIELD_PLATE_ID, FIELD_LABELS,
  FIELD_COLLISION, FIELD_TYPE_BITMAP, FIELD_DIV_BITMAP, FIELD_SORT_KEYS, FIELD_SORT_VALS,
@@ -279,6 +280,7 @@ def _declare(L: C.CDLL) -> None:
         "tecto_server_run_trace_sequential": ([P, C.POINTER(Request), C.c_int, P, C.POINTER(RequestResult),
                                                C.POINTER(ServerStats)], C.c_int),
         "tecto_server_set_dry_cost": ([P, C.c_double], C.c_int),
+        "tecto_server_set_init": ([P, C.c_int], C.c_int),
         "tecto_server_set_output": ([P, C.c_char_p, C.c_int, C.c_float, C.c_float], C.c_int),
         "tecto_selftest_div": ([P, P, P, C.c_size_t, P], C.c_int),
         "tecto_png_encode": ([P, C.c_int, C.c_int, C.c_int, P, C.c_size_t, C.POINTER(C.c_size_t)], C.c_int),
@@ -677,6 +679,10 @@ class Server:
         """Write finished requests' exports and snapshots (SERVER_OUT_* bits) into `directory`."""
         d = os.fsencode(directory) if directory is not None else None
         check(lib().tecto_server_set_output(self.ptr, d, what, height_min, height_max), "tecto_server_set_output")
+
+    def set_init(self, mode: int) -> None:
+        """SERVER_INIT_SYNTHETIC (default) or SERVER_INIT_REFERENCE for admitted worlds."""
+        check(lib().tecto_server_set_init(self.ptr, mode), "tecto_server_set_init")
 
     def set_dry_cost(self, seconds_per_mcell_step: float) -> None:
         check(lib().tecto_server_set_dry_cost(self.ptr, seconds_per_mcell_step), "tecto_server_set_dry_cost")

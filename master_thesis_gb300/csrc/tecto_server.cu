@@ -33,6 +33,7 @@ struct tecto_server {
     tecto_batch *batch = nullptr;
     std::string out_dir;     // where finished requests are written (tecto_server_set_output)
     int out_what = 0;        // TECTO_SERVER_OUT_* bits
+    int init_mode = TECTO_SERVER_INIT_SYNTHETIC;
     float out_lo = 0.0f, out_hi = 1.0f;  // height range of the 16-bit export
 };
 
@@ -87,9 +88,14 @@ void finish_stats(const tecto_request *req, int n, const tecto_request_result *r
 
 int make_world(tecto_server *sv, const tecto_request &r, cudaStream_t st, tecto_world **out)
 {
-    int rc = tecto_world_create(&sv->settings, r.width, r.height, r.worldSeed, out);
+    tecto_settings ws = sv->settings;
+    if (sv->init_mode == TECTO_SERVER_INIT_REFERENCE) ws.sim.numStartingPlates = r.plates;
+    int rc = tecto_world_create(&ws, r.width, r.height, r.worldSeed, out);
     if (rc != TECTO_OK) return rc;
-    rc = tecto_world_init_synthetic_device(*out, r.plates, r.velRange, r.genSeed, (tecto_stream_t)st);
+    if (sv->init_mode == TECTO_SERVER_INIT_REFERENCE)
+        rc = tecto_world_init_reference(*out, (tecto_stream_t)st);
+    else
+        rc = tecto_world_init_synthetic_device(*out, r.plates, r.velRange, r.genSeed, (tecto_stream_t)st);
     if (rc != TECTO_OK) {
         tecto_world_destroy(*out);
         *out = nullptr;
@@ -178,6 +184,16 @@ int tecto_server_set_output(tecto_server *server, const char *directory, int wha
     server->out_what = what;
     server->out_lo = height_min;
     server->out_hi = height_max;
+    return TECTO_OK;
+}
+
+int tecto_server_set_init(tecto_server *server, int mode)
+{
+    if (!server || (mode != TECTO_SERVER_INIT_SYNTHETIC && mode != TECTO_SERVER_INIT_REFERENCE)) {
+        set_error("tecto_server_set_init: invalid argument");
+        return TECTO_ERR_INVALID;
+    }
+    server->init_mode = mode;
     return TECTO_OK;
 }
 

@@ -65,3 +65,23 @@ def test_initialised_world_steps_like_the_oracle(stream):
         o.step(1)
         np.testing.assert_array_equal(w.download(T.FIELD_PLATE_ID, stream), o.id, err_msg=f"ids step {step}")
         np.testing.assert_array_equal(w.download(T.FIELD_HEIGHT, stream), o.h, err_msg=f"heights step {step}")
+
+
+def test_server_admits_reference_initialised_worlds(stream):
+    """Served requests initialised with the reference's initialisation give the same worlds as
+    initialising and stepping them directly."""
+    s = settings(1, (40,))
+    reqs = [T.Request(width=W, height=H, plates=p, steps=st, velRange=1.0, genSeed=0, worldSeed=500 + i,
+                      arrival_s=0.001 * i)
+            for i, (W, H, p, st) in enumerate([(64, 64, 6, 3), (96, 48, 4, 2), (80, 80, 9, 4)])]
+    sv = T.Server(s, 3 * T.world_bytes(96, 80), max_worlds=3)
+    sv.set_init(T.SERVER_INIT_REFERENCE)
+    res, st = sv.run_trace(reqs, stream)
+    assert st.completed == 3
+    for i, q in enumerate(reqs):
+        ws = settings(q.plates, (40,))
+        w = T.World(ws, q.width, q.height, seed=q.worldSeed)
+        w.init_reference(stream)
+        w.step(q.steps, stream)
+        assert np.float32(w.download(T.FIELD_HEIGHT, stream).astype(np.float64).sum()) == res[i].height_checksum
+    sv.close()
