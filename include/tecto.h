@@ -142,8 +142,15 @@ typedef struct tecto_step_settings {
                                  per SM, up to 2 */
     int plateDynamics;        /* TECTO_PLATE_DYNAMICS_*: 0 fixed plate velocities (the benchmark), 1 the
                                  reference's applyPlateMovementChanges after every step */
-    int reserved[4];
+    int platePolicy;          /* TECTO_PLATE_RELABEL | TECTO_PLATE_MERGE bits, 0 = neither */
+    int reserved[3];
 } tecto_step_settings;
+
+/* Plate policy after a step (bits of platePolicy). */
+#define TECTO_PLATE_RELABEL 1 /* after each CCL: fragments of a plate other than its largest take free
+                                 plate ids or their neighbours' (applyCCL, plate_tectonic_sim.cu:391-467) */
+#define TECTO_PLATE_MERGE 2   /* after every step: touching plates that move alike merge (mergePlates,
+                                 plate_tectonic_sim.cu:470-494) */
 
 /* Plate dynamics modes. */
 #define TECTO_PLATE_DYNAMICS_OFF 0

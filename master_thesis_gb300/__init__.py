@@ -34,6 +34,7 @@ NUM_DIV_WORDS = 1013
 UPLIFT_GAUSSIAN, UPLIFT_NONE, UPLIFT_REFERENCE = 0, 1, 2
 CCL_4, CCL_8, CCL_REF8 = 4, 8, 9
 PLATE_DYNAMICS_OFF, PLATE_DYNAMICS_REFERENCE = 0, 1
+PLATE_RELABEL, PLATE_MERGE = 1, 2
 PNG_GRAY16, PNG_RGB8, PNG_GRAY8 = 0, 1, 2
 EXPORT_HEIGHT_GRAY16, EXPORT_PLATES_RGB = 0, 1
 SERVER_OUT_HEIGHT_PNG, SERVER_OUT_PLATES_PNG, SERVER_OUT_SNAPSHOT = 1, 2, 4
@@ -126,7 +127,8 @@ class StepSettings(C.Structure):
         ("hydraulicTile", C.c_int),
         ("thermalTile", C.c_int),
         ("plateDynamics", C.c_int),
-        ("reserved", C.c_int * 4),
+        ("platePolicy", C.c_int),
+        ("reserved", C.c_int * 3),
     ]
 
 

@@ -27,6 +27,7 @@ SOURCES = [
     "k_sort_noalloc.cu",
     "k_collide.cu",
     "k_dynamics.cu",
+    "k_policy.cu",
     "k_resolve.cu",
     "k_erosion.cu",
     "k_ccl.cu",

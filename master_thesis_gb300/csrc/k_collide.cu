@@ -204,8 +204,10 @@ int launch_plates(Batch &b, cudaStream_t st)
     }
     int rc = launch_clear_marks(b, st);  // must run before k_plates resets the list count
     if (rc != TECTO_OK) return rc;
-    if (dyn && (rc = launch_plate_stats(b, st)) != TECTO_OK) return rc;
-    k_plates<<<(unsigned)b.members.size(), 256, 0, st>>>(b.d_worlds, dyn);
+    // plate dynamics and the plate policy read the per-plate mass, size and centre of the step
+    const int stats = dyn != TECTO_PLATE_DYNAMICS_OFF || b.settings.step.platePolicy != 0;
+    if (stats && (rc = launch_plate_stats(b, st)) != TECTO_OK) return rc;
+    k_plates<<<(unsigned)b.members.size(), 256, 0, st>>>(b.d_worlds, stats);
     TECTO_CUDA(cudaGetLastError());
     b.launches += 1;
     return TECTO_OK;

@@ -152,7 +152,7 @@ const Field kKernelFields[] = {
 const Field kStepFields[] = {SI(hydraulicIterations), SF(hydraulicDt), SI(thermalIterations),
                              SI(upliftMode), SF(upliftAmount), SF(upliftSigma), SI(upliftRadius),
                              SI(cclConnectivity), SI(sortRadixBits), SI(hydraulicTile), SI(thermalTile),
-                             SI(plateDynamics)};
+                             SI(plateDynamics), SI(platePolicy)};
 #undef SF
 #undef SI
 const Field kSimFields[] = {{"numStartingPlates", 'i', offsetof(tecto_simulation_settings, numStartingPlates)},

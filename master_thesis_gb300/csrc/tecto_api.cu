@@ -145,7 +145,7 @@ size_t world_footprint(int W, int H)
     L.add(kPairs); L.add(kDivWords * 4); L.add(kDivWords * 4); L.add(kPairs * sizeof(PairCounts));
     L.add(kPlates * sizeof(tecto_plate)); L.add(kPlates * sizeof(tecto_plate));
     L.add((kPlates + 1) * sizeof(int2)); L.add(kPlates * sizeof(tecto_plate_dynamics));
-    L.add(kPlates * sizeof(PlateAcc)); L.add(sizeof(Control));
+    L.add(kPlates * sizeof(PlateAcc)); L.add(sizeof(PolicyState)); L.add(sizeof(Control));
     // its share of a batch's sort: key/value ping-pong plus the scratch of the widest digit choice
     size_t scratch = 0;
     for (int rb = 8; rb <= kMaxRadixBits; ++rb)
@@ -213,6 +213,7 @@ int tecto_world_create(const tecto_settings *settings, int width, int height, ui
     const size_t o_off = L.add((kPlates + 1) * sizeof(int2));
     const size_t o_dyn = L.add(kPlates * sizeof(tecto_plate_dynamics));
     const size_t o_pacc = L.add(kPlates * sizeof(PlateAcc));
+    const size_t o_pol = L.add(sizeof(PolicyState));
     const size_t o_ctl = L.add(sizeof(Control));
     cudaError_t e = cudaMalloc(&w->arena, L.total);
     if (e != cudaSuccess) {
@@ -253,6 +254,7 @@ int tecto_world_create(const tecto_settings *settings, int width, int height, ui
     d.off = (int2 *)(base + o_off);
     d.dyn = (tecto_plate_dynamics *)(base + o_dyn);
     d.pacc = (PlateAcc *)(base + o_pacc);
+    d.policy = (PolicyState *)(base + o_pol);
     d.pressure = nullptr;
     d.pw = d.ph = 0;
     d.ctl = (Control *)(base + o_ctl);
@@ -755,6 +757,7 @@ int tecto_phase_finish(tecto_world *w, tecto_stream_t stream)
     const bool due = w->iteration % (uint32_t)period == 0;
     if ((rc = launch_finish(*b, st)) == TECTO_OK &&
         (!due || (rc = launch_ccl(*b, w->settings.step.cclConnectivity, false, st)) == TECTO_OK) &&
+        (!w->settings.step.platePolicy || (rc = launch_plate_policy(*b, due ? 1 : 0, st)) == TECTO_OK) &&
         (rc = launch_bump_iteration(*b, st)) == TECTO_OK)
         w->iteration += 1;
     TECTO_PHASE_EPILOGUE

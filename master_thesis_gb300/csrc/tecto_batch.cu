@@ -252,6 +252,7 @@ int batch_enqueue_step(Batch &b, cudaStream_t st, int ccl)
     if ((rc = launch_hydraulic(b, s.step.hydraulicIterations, s.step.hydraulicDt, st)) != TECTO_OK) return rc;
     if ((rc = launch_finish(b, st)) != TECTO_OK) return rc;
     if (ccl && (rc = launch_ccl(b, s.step.cclConnectivity, ccl == 2, st)) != TECTO_OK) return rc;
+    if (s.step.platePolicy && (rc = launch_plate_policy(b, ccl, st)) != TECTO_OK) return rc;
     return launch_bump_iteration(b, st);
 }
 

@@ -51,7 +51,11 @@ struct Control {
     uint32_t seed;          // PlateTectonicSim::m_seed
     uint32_t error;         // kErr* bits
     uint32_t acc_count;     // entries in this world's accretion list for the current step
-    uint32_t pad[12];
+    uint32_t comp_count;    // plate relabel: components listed this step
+    uint32_t unassigned;    // plate relabel: cells without an id after the lookup
+    uint32_t unresolved;    // plate relabel: cells the neighbour fill could not reach (last relabel)
+    uint32_t merges;        // plate merges of the last step
+    uint32_t pad[8];
 };
 
 // Per-batch device control block.
@@ -90,6 +94,16 @@ constexpr float kFricLimit = 4194304.0f;           // |friction term| clamp, 2^2
 constexpr int kStatTileX = 256, kStatTileY = 64;   // TK_STATS tile
 constexpr float kTwoPiF = 6.28318548202514648f;    // CURAND_2PI as a float
 
+// Per-world state of the plate policy (relabel and merges).
+struct PolicyState {
+    int max_count[256];                // per plate: cells of its largest component
+    int merge_ids[256];                // getPlateMerges' table: 0, -1 parent, 255 - parent for a child
+    uint32_t neighbors[kDivWords];     // plate pairs that touch (triangle bits)
+    unsigned long long top[256];       // ranked components (count << 32 | label)
+    int any_merge;
+    int pad[63];
+};
+
 // Device descriptor of one world (one cudaMalloc'd arena per world, structure of arrays).
 struct WorldDev {
     int W, H;
@@ -117,6 +131,7 @@ struct WorldDev {
     int2 *off;              // [kPlates + 1] this step's integer displacement per plate
     tecto_plate_dynamics *dyn;  // [kPlates] plate dynamics records
     PlateAcc *pacc;         // [kPlates] plate dynamics sums of the current step
+    PolicyState *policy;    // plate relabel and merges
     const float *pressure;  // asthenosphere pressure texture (pw x ph), or null
     int pw, ph;
     Control *ctl;
@@ -294,6 +309,9 @@ int launch_finish(Batch &b, cudaStream_t st);
 // applyPlateMovementChanges at its end
 int launch_plate_stats(Batch &b, cudaStream_t st);
 int launch_plate_motion(Batch &b, cudaStream_t st);
+// plate policy after a step (TECTO_PLATE_RELABEL / TECTO_PLATE_MERGE): ccl 0 no labelling ran, 1 it
+// ran for the world (single world), 2 per world when due (batch)
+int launch_plate_policy(Batch &b, int ccl, cudaStream_t st);
 int launch_clear_marks(Batch &b, cudaStream_t st);
 int launch_bump_iteration(Batch &b, cudaStream_t st);
 // due_only: skip worlds whose step counter is not a multiple of iterationsForCCL

@@ -128,6 +128,8 @@ def lib() -> C.CDLL:
         L.or_plate_motion.argtypes = [C.c_int, C.c_int, V, V, V, V, C.c_int, C.c_int, V]
         L.or_reference_seeds.argtypes = [C.c_int, C.c_int, C.c_uint32, C.c_int, V, C.c_int, V, V, V, C.c_int, V, V, V]
         L.or_init_reference.argtypes = [C.c_int, C.c_int, C.c_uint32, V, V, V, C.c_int, V, V]
+        L.or_relabel.argtypes = [C.c_int, C.c_int, V, V, V, V, C.c_int]
+        L.or_merge.argtypes = [C.c_int, C.c_int, V, V, V, V, V]
         L.or_hash.argtypes = [C.c_uint32]
         L.or_hash.restype = C.c_uint32
         L.or_simplex3.argtypes = [C.c_float] * 4 + [C.c_int]
@@ -176,6 +178,7 @@ def ref() -> C.CDLL:
         L.ref_curl.argtypes = [C.c_int, C.c_int, V, C.c_int, C.c_int, V]
         L.ref_plate_motion.argtypes = [C.c_int, C.c_int, V, V, V, V]
         L.ref_init.argtypes = [C.c_int, C.c_int, C.c_int, V, V, V, C.c_int, V, V]
+        L.ref_merges.argtypes = [C.c_int, C.c_int, V, V, V, V, V]
         L.ref_ids_rgb.argtypes = [C.c_int, C.c_int, V, V]
         _r = L
     return _r
@@ -277,6 +280,23 @@ def init_reference(W, H, seed, sx, sy, sid):
     sx, sy, sid = (np.ascontiguousarray(a, t) for a, t in ((sx, np.float32), (sy, np.float32), (sid, np.uint8)))
     lib().or_init_reference(W, H, seed, _P(sx), _P(sy), _P(sid), len(sx), _P(h), _P(ids))
     return h, ids
+
+
+def relabel(ids, labels, plates, dyn, min_plate_size):
+    """or_relabel on copies: (ids, plates, dyn, cells left without an id)."""
+    i, pl, dy = np.ascontiguousarray(ids, np.uint8).copy(), plates.copy(), dyn.copy()
+    lab = np.ascontiguousarray(labels, np.uint32)
+    H, W = i.shape
+    left = lib().or_relabel(W, H, _P(i), _P(lab), _P(pl), _P(dy), min_plate_size)
+    return i, pl, dy, left
+
+
+def merge(ids, plates, dyn, bitmap, settings):
+    """or_merge on copies: (ids, bitmap, merges)."""
+    i, bm = np.ascontiguousarray(ids, np.uint8).copy(), np.ascontiguousarray(bitmap, np.uint8).copy()
+    H, W = i.shape
+    n = lib().or_merge(W, H, _P(i), _P(plates), _P(dyn), _P(bm), C.addressof(settings.kernel))
+    return i, bm, n
 
 
 def plate_stats(h, ids, iteration, dyn=None):

@@ -411,4 +411,40 @@ void ref_init(int W, int H, int seed, const float *sx, const float *sy, const ui
     launch(blocks_for((size_t)W * H), TPB, [&] { initHeightmap(&tH, seed, 4); });
 }
 
+/* mergePlates (plate_tectonic_sim.cu:470-494) with the reference's kernels: getNeighboringPlates,
+ * getPlateMerges (its threads in ascending order; the device-side launch of clearCollisionTypes is
+ * not compiled here, so clearCollisionTypes runs afterwards for each parent), then
+ * mergeAndCountSizeMass for the id remap (its per-block sums, which need a real barrier, are
+ * discarded).  merge_ids[255] receives getPlateMerges' table. */
+void ref_merges(int W, int H, uint8_t *ids, const tecto_plate *plates, const tecto_plate_dynamics *dyn,
+                uint8_t *type_bitmap, int *merge_ids)
+{
+    const size_t N = (size_t)W * H;
+    auto pd = make_plates(plates);
+    for (unsigned k = 0; k < MAX_PLATE_COUNT; ++k) {
+        pd[k].velocitySmoothed = dyn[k].velocitySmoothed;
+        pd[k].directionSmoothed = Vec2<float>(dyn[k].directionSmoothed_x, dyn[k].directionSmoothed_y);
+        pd[k].mass = dyn[k].mass;
+        pd[k].size = dyn[k].size;
+        pd[k].mergeWaitTime = dyn[k].mergeWaitTime;
+    }
+    std::vector<uint8_t> nbm((size_t)MAX_PLATE_COUNT * MAX_PLATE_COUNT, 0);
+    bool *nb = reinterpret_cast<bool *>(nbm.data());
+    CudaTexture<uint8_t> tId(ids, Vec2<int>(W, H));
+    CudaTexture<bool> tNb(nb, Vec2<int>(MAX_PLATE_COUNT, MAX_PLATE_COUNT));
+    CudaTexture<uint8_t> tBm(type_bitmap, Vec2<int>(NUM_TRIANGLE_ENTRIES, 1));
+    std::memset(merge_ids, 0, sizeof(int) * MAX_PLATE_COUNT);
+    launch(blocks_for(N), TPB, [&] { getNeighboringPlates(&tId, &tNb); });
+    launch(blocks_for((size_t)MAX_PLATE_COUNT * MAX_PLATE_COUNT), TPB,
+           [&] { getPlateMerges(&tNb, pd.data(), merge_ids, &tBm); });
+    for (unsigned k = 0; k < MAX_PLATE_COUNT; ++k)
+        if (merge_ids[k] == -1) launch(1, TPB, [&] { clearCollisionTypes(tBm, (int)k); });
+    std::vector<Vec2<float>> slope(N);
+    CudaTexture<Vec2<float>> tSlope(slope.data(), Vec2<int>(W, H));
+    std::vector<float> hz(N, 0.0f);
+    CudaTexture<float> tH(hz.data(), Vec2<int>(W, H));
+    auto scratch = pd;
+    launch(blocks_for(N), TPB, [&] { mergeAndCountSizeMass(&tId, &tH, merge_ids, scratch.data(), &tSlope); });
+}
+
 } // extern "C"

@@ -1167,9 +1167,10 @@ void or_step_dyn(int W, int H, float *h, float *w, float *s, float *flux, uint8_
     float *hn = (float *)malloc(N * sizeof(float));
     uint8_t *idn = (uint8_t *)malloc(N);
     const int dynamics = dyn && st->step.plateDynamics == TECTO_PLATE_DYNAMICS_REFERENCE;
+    const int policy = dyn ? st->step.platePolicy & (TECTO_PLATE_RELABEL | TECTO_PLATE_MERGE) : 0;
     int64_t fric[NPLATE];
     memset(fric, 0, sizeof(fric));
-    if (dynamics) or_plate_stats(W, H, h, id, *iteration, dyn);
+    if (dynamics || policy) or_plate_stats(W, H, h, id, *iteration, dyn);
     float *uh = NULL;
     uint8_t *ut = NULL;
     if (st->step.upliftMode == TECTO_UPLIFT_REFERENCE) {
@@ -1194,7 +1195,11 @@ void or_step_dyn(int W, int H, float *h, float *w, float *s, float *flux, uint8_
     if (dynamics) or_plate_motion(W, H, plates, dyn, fric, pressure, pw, ph, &st->kernel);
     or_accretion(W, H, h, acc, id, &st->kernel);
     const int period = st->sim.iterationsForCCL > 0 ? st->sim.iterationsForCCL : 1;
-    if (*iteration % (uint32_t)period == 0) or_ccl(W, H, id, labels, st->step.cclConnectivity);
+    const int ccl_due = *iteration % (uint32_t)period == 0;
+    if (ccl_due) or_ccl(W, H, id, labels, st->step.cclConnectivity);
+    if (ccl_due && (policy & TECTO_PLATE_RELABEL))
+        or_relabel(W, H, id, labels, plates, dyn, st->kernel.minPlateSize);
+    if (policy & TECTO_PLATE_MERGE) or_merge(W, H, id, plates, dyn, bm, &st->kernel);
     *iteration += 1;
 }
 
@@ -1404,4 +1409,167 @@ void or_init_reference(int W, int H, uint32_t seed, const float *sx, const float
             }
             h[i] = 5000.0f + value * (15000.0f - 5000.0f);
         }
+}
+
+/* ---- plate relabel and merges ------------------------------------------------------------------ */
+
+static int cmp_u64_desc(const void *a, const void *b)
+{
+    const uint64_t x = *(const uint64_t *)a, y = *(const uint64_t *)b;
+    return x < y ? 1 : (x > y ? -1 : 0);
+}
+
+/* applyCCL's relabel (plate_tectonic_sim.cu:391-467; createPlateIdLabelMap, getMaxSizeLabels,
+ * createLabelIdLookup, postCClIdReassign, assignUnassignedIdsToNeighbor :1394-1405, :3114-3206,
+ * :2052-2101).  Components (CCL labels: the minimum cell index of each) are ranked by cell count,
+ * larger first, ties by the larger label (the reference's sort by label and then by count).  Of the
+ * first min(255, components): a component as large as its plate's largest keeps the plate's id;
+ * a smaller one of at least minPlateSize cells takes the next free id (ascending among the ids below
+ * min(255, components) whose plate has no cells), with a copy of the plate's records; any other
+ * component loses its id.  Cells without an id then take the most frequent id among their eight
+ * neighbours (first in the order +x, -x, +y, -y, +x+y, +x-y, -x+y, -x-y on ties), in rounds that
+ * each read the ids of the round before, until none is left or a round assigns nothing.  Returns
+ * the number of cells left without an id. */
+int or_relabel(int W, int H, uint8_t *id, const uint32_t *labels, tecto_plate *plates, tecto_plate_dynamics *dyn,
+               int minPlateSize)
+{
+    const size_t N = (size_t)W * (size_t)H;
+    uint32_t *count = (uint32_t *)calloc(N, sizeof(uint32_t));
+    for (size_t i = 0; i < N; ++i) count[labels[i]] += 1;
+    size_t M = 0;
+    for (size_t i = 0; i < N; ++i)
+        if (labels[i] == i) ++M;
+    uint64_t *keys = (uint64_t *)malloc(sizeof(uint64_t) * (M ? M : 1));
+    int max_count[256];
+    memset(max_count, 0, sizeof(max_count));
+    size_t m = 0;
+    for (size_t i = 0; i < N; ++i)
+        if (labels[i] == i) {
+            keys[m++] = ((uint64_t)count[i] << 32) | (uint64_t)i;
+            if ((int)count[i] > max_count[id[i]]) max_count[id[i]] = (int)count[i];
+        }
+    qsort(keys, M, sizeof(uint64_t), cmp_u64_desc);
+    const int ntop = M < NPLATE ? (int)M : (int)NPLATE;
+    int avail[NPLATE], navail = 0, next = 0;
+    for (int k = 0; k < ntop; ++k)
+        if (dyn[k].size == 0) avail[navail++] = k;
+    uint8_t *lookup = (uint8_t *)malloc(N);  /* by root cell */
+    for (size_t i = 0; i < N; ++i)
+        if (labels[i] == i) lookup[i] = (uint8_t)NPLATE;
+    for (int t = 0; t < ntop; ++t) {
+        const uint32_t label = (uint32_t)(keys[t] & 0xFFFFFFFFu);
+        const int c = (int)(keys[t] >> 32);
+        const uint8_t plate = id[label];
+        if (c == max_count[plate]) {
+            lookup[label] = plate;
+        } else if (c >= minPlateSize && next < navail) {
+            const int nid = avail[next++];
+            plates[nid] = plates[plate];
+            dyn[nid] = dyn[plate];
+            lookup[label] = (uint8_t)nid;
+        }
+    }
+    size_t left = 0;
+    for (size_t i = 0; i < N; ++i) {
+        id[i] = lookup[labels[i]];
+        if (id[i] == NPLATE) ++left;
+    }
+    static const int OX[8] = {1, -1, 0, 0, 1, 1, -1, -1}, OY[8] = {0, 0, 1, -1, 1, -1, 1, -1};
+    uint8_t *pending = (uint8_t *)malloc(N);
+    while (left > 0) {
+        size_t assigned = 0;
+        for (size_t i = 0; i < N; ++i) {
+            pending[i] = (uint8_t)NPLATE;
+            if (id[i] != NPLATE) continue;
+            const int x = (int)(i % (size_t)W), y = (int)(i / (size_t)W);
+            uint8_t nb[8];
+            int n = 0;
+            for (int k = 0; k < 8; ++k) {
+                const uint8_t v = id[cidx(x + OX[k], y + OY[k], W, H)];
+                if (v != NPLATE) nb[n++] = v;
+            }
+            int best = 0;
+            uint8_t sel = (uint8_t)NPLATE;
+            for (int a = 0; a < n; ++a) {
+                int c = 1;
+                for (int b = 0; b < n; ++b)
+                    if (a != b && nb[b] == nb[a]) ++c;
+                if (c > best) {
+                    best = c;
+                    sel = nb[a];
+                }
+            }
+            pending[i] = sel;
+        }
+        for (size_t i = 0; i < N; ++i)
+            if (pending[i] != NPLATE) {
+                id[i] = pending[i];
+                ++assigned;
+            }
+        left -= assigned;
+        if (assigned == 0) break;
+    }
+    free(pending);
+    free(lookup);
+    free(keys);
+    free(count);
+    return (int)left;
+}
+
+/* mergePlates (plate_tectonic_sim.cu:470-494): getNeighboringPlates (:1283-1311) marks the plate
+ * pairs that touch across a +x or +y cell edge; getPlateMerges (:1313-1379) takes the pairs in
+ * ascending (max, min) order: two touching plates merge when both move no faster than
+ * mergeMinVelocity, or when their smoothed directions agree (dot >= mergeDotDirectionThreshold) and
+ * their smoothed speeds differ by at most mergeVelocityDiffThreshold; not while either waits
+ * (mergeWaitTime) nor above targetMaximumPlateArea together; each plate merges at most once; the
+ * heavier (ties: the lower id) is the parent.  Each merge clears the collision-type bitmap
+ * entries clearCollisionTypes (:1381-1392) addresses: it indexes the 1-D triangle array with
+ * (min(parent, k), max(parent, k)), which lands on entry min(parent, k), so entries 0..parent-1 and,
+ * for a parent below 254, entry parent.  mergeAndCountSizeMass (:100-135) then gives each child's
+ * cells the parent's id.  Returns the number of merges. */
+int or_merge(int W, int H, uint8_t *id, const tecto_plate *plates, const tecto_plate_dynamics *dyn,
+             uint8_t *type_bitmap, const tecto_kernel_settings *ks)
+{
+    static uint8_t nb[NPLATE * NPLATE];
+    memset(nb, 0, sizeof(nb));
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const uint8_t c = id[(size_t)y * W + x];
+            const uint8_t r = id[cidx(x + 1, y, W, H)], t = id[cidx(x, y + 1, W, H)];
+            if (c != r && c != NPLATE && r != NPLATE)
+                nb[(r < c ? c : r) * NPLATE + (r < c ? r : c)] = 1;
+            if (c != t && c != NPLATE && t != NPLATE)
+                nb[(t < c ? c : t) * NPLATE + (t < c ? t : c)] = 1;
+        }
+    int merge_ids[NPLATE];
+    memset(merge_ids, 0, sizeof(merge_ids));
+    int merges = 0;
+    for (int idx = 0; idx < (int)(NPLATE * NPLATE); ++idx) {
+        const int x = idx % (int)NPLATE, y = idx / (int)NPLATE;
+        if (x >= y || !nb[idx]) continue;
+        const float dot = dyn[x].directionSmoothed_x * dyn[y].directionSmoothed_x +
+                          dyn[x].directionSmoothed_y * dyn[y].directionSmoothed_y;
+        const float vdiff = fabsf(dyn[x].velocitySmoothed - dyn[y].velocitySmoothed);
+        if (!(plates[x].velocity <= ks->mergeMinVelocity && plates[y].velocity <= ks->mergeMinVelocity) &&
+            !(dot >= ks->mergeDotDirectionThreshold && vdiff <= ks->mergeVelocityDiffThreshold))
+            continue;
+        if (dyn[x].mergeWaitTime > 0 || dyn[y].mergeWaitTime > 0) continue;
+        if (dyn[x].size + dyn[y].size > ks->targetMaximumPlateArea) continue;
+        const int x_parent = dyn[y].mass <= dyn[x].mass;
+        if (merge_ids[x] != 0) continue;
+        merge_ids[x] = x_parent ? -1 : (int)NPLATE - y;
+        if (merge_ids[y] != 0) {
+            merge_ids[x] = 0;
+            continue;
+        }
+        merge_ids[y] = x_parent ? (int)NPLATE - x : -1;
+        const int parent = x_parent ? x : y;
+        for (int k = 0; k < (int)NPLATE; ++k)
+            if (k != parent) type_bitmap[k < parent ? k : parent] = 0;
+        ++merges;
+    }
+    const size_t N = (size_t)W * (size_t)H;
+    for (size_t i = 0; i < N; ++i)
+        if (id[i] != NPLATE && merge_ids[id[i]] > 0) id[i] = (uint8_t)((int)NPLATE - merge_ids[id[i]]);
+    return merges;
 }

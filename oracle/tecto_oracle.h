@@ -114,6 +114,13 @@ int or_reference_seeds(int W, int H, uint32_t seed, int numPlates, const int *ge
 void or_init_reference(int W, int H, uint32_t seed, const float *sx, const float *sy, const uint8_t *sid, int S,
                        float *h, uint8_t *id);
 
+/* Plate policy after a step: applyCCL's relabel of plate fragments (returns cells left without an
+ * id) and mergePlates (returns merges). */
+int or_relabel(int W, int H, uint8_t *id, const uint32_t *labels, tecto_plate *plates, tecto_plate_dynamics *dyn,
+               int minPlateSize);
+int or_merge(int W, int H, uint8_t *id, const tecto_plate *plates, const tecto_plate_dynamics *dyn,
+             uint8_t *type_bitmap, const tecto_kernel_settings *ks);
+
 /* Building blocks exposed for unit tests. */
 uint32_t or_hash(uint32_t v);
 float or_simplex3(float x, float y, float z, float scale, int seed);

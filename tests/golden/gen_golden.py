@@ -305,6 +305,44 @@ def ref_init(name):
     print("wrote", name)
 
 
+def ref_policy(name):
+    """mergePlates with the reference's kernels (getNeighboringPlates, getPlateMerges in thread order,
+    clearCollisionTypes per parent, the remap of mergeAndCountSizeMass) on a ten-plate map whose
+    records make some pairs merge, some compete for the same plate, one wait and one exceed the
+    area cap."""
+    R = O.ref()
+    st = T.baseline_settings()
+    st.kernel.mergeMinVelocity = 0.2
+    st.kernel.mergeDotDirectionThreshold = 0.9
+    st.kernel.mergeVelocityDiffThreshold = 0.1
+    st.kernel.targetMaximumPlateArea = 900
+    R.ref_set_settings(C.addressof(st.kernel))
+    W, H = 60, 40
+    _, ids, _ = T.generate_world(W, H, 10, 1.0, 31)
+    rng = np.random.default_rng(37)
+    pl = np.zeros(255, T.PLATE_DTYPE)
+    dy = np.zeros(255, T.PLATE_DYNAMICS_DTYPE)
+    ang = rng.uniform(0, 2 * np.pi, 10)
+    ang[[1, 2, 3]] = ang[0] + rng.uniform(-0.2, 0.2, 3)  # aligned with plate 0
+    for k in range(10):
+        pl[k]["velocity"] = rng.uniform(0.05, 0.6)
+        pl[k]["direction_x"], pl[k]["direction_y"] = np.cos(ang[k]), np.sin(ang[k])
+        dy[k]["velocitySmoothed"] = pl[k]["velocity"] + rng.uniform(-0.05, 0.05)
+        dy[k]["directionSmoothed_x"], dy[k]["directionSmoothed_y"] = np.cos(ang[k]), np.sin(ang[k])
+        dy[k]["size"] = int((ids == k).sum())
+        dy[k]["mass"] = float(rng.uniform(100, 1000))
+    dy[7]["mergeWaitTime"] = 2
+    pl[[5, 6]]["velocity"] = 0.1  # slow pair candidates
+    bitmap = rng.integers(0, 256, 32385).astype(np.uint8)
+    out_ids, out_bm = ids.copy(), bitmap.copy()
+    merge_ids = np.zeros(255, np.int32)
+    R.ref_merges(W, H, P(out_ids), P(pl), P(dy), P(out_bm), P(merge_ids))
+    np.savez_compressed(OUT / f"{name}.npz", ids=ids, plates=pl, dyn=dy, bitmap=bitmap, out_ids=out_ids,
+                        out_bitmap=out_bm, merge_ids=merge_ids,
+                        ks=np.float32([0.2, 0.9, 0.1, 900]))
+    print("wrote", name, "merges", int((merge_ids == -1).sum()))
+
+
 def main():
     O.build(ref=True)
     ref_step_composition("ref_steps_baseline_64x64", 64, 64, 8, 1.0, 7, "baseline", 6, 20, 0.02)
@@ -316,6 +354,7 @@ def main():
     ref_export("ref_export")
     ref_dynamics("ref_dynamics")
     ref_init("ref_init")
+    ref_policy("ref_policy")
 
 
 if __name__ == "__main__":
