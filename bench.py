@@ -19,7 +19,8 @@ and sort digit width picked by the autotuner.  Beside it:
                cell-updates/s, and a saturated trace (all requests at t=0) for capacity;
   plain_2048   one 2048^2 world, 32 plates (plain path; its k_hydro roofline);
   plain_8192   one 8192^2 world, 64 plates, velocities in [-2, 2], 8-connected CCL every step.
-`e2e` repeats the headline through the C ABI with host buffers: every step uploads each world's
+`e2e` repeats the headline through the C ABI with host buffers (packed: one buffer per field for all
+worlds, tecto_batch_upload_async / download_async): every step uploads each world's
 state from pinned host memory, steps the batch, downloads heights and plate ids, and waits for them.
 Reference arm: the reference path's CPU implementation (the oracle's C restatement, all host
 threads) on a bounded sample of the same mixed-size workload.  With N > 1 (torchrun) every rank
@@ -358,20 +359,21 @@ def run_engine(args, ws, rank, local):
     sp = stream.cuda_stream
     up_fields = (T.FIELD_HEIGHT, T.FIELD_WATER, T.FIELD_SEDIMENT, T.FIELD_FLUX, T.FIELD_PLATE_ID)
     down_fields = (T.FIELD_HEIGHT, T.FIELD_PLATE_ID)
-    hosts = [{f: torch.from_numpy(w.download(f)).pin_memory() for f in up_fields} for w in worlds]
-    outs = [{f: torch.empty_like(h[f]).pin_memory() for f in down_fields} for h in hosts]
+    # one packed pinned host buffer per field, the worlds in batch order
+    hosts = [{f: torch.from_numpy(np.concatenate([w.download(f).ravel() for w in worlds])).pin_memory()
+              for f in up_fields}]
+    outs = [{f: torch.empty_like(hosts[0][f]).pin_memory() for f in down_fields}]
 
     def e2e_step():
-        # stream-ordered copies from / to pinned host buffers, one wait per step
-        for w, hs in zip(worlds, hosts):
-            for f, t in hs.items():
-                T.check(L.tecto_world_upload_async(w.ptr, f, t.data_ptr(), t.numel() * t.element_size(), sp),
-                        "upload")
+        # stream-ordered packed copies from / to pinned host buffers (one copy and one device
+        # scatter / gather per field for all worlds), one wait per step
+        for f, t in hosts[0].items():
+            T.check(L.tecto_batch_upload_async(batch.ptr, f, t.data_ptr(), t.numel() * t.element_size(), sp),
+                    "upload")
         batch.step(1, stream)
-        for w, os_ in zip(worlds, outs):
-            for f, t in os_.items():
-                T.check(L.tecto_world_download_async(w.ptr, f, t.data_ptr(), t.numel() * t.element_size(), sp),
-                        "download")
+        for f, t in outs[0].items():
+            T.check(L.tecto_batch_download_async(batch.ptr, f, t.data_ptr(), t.numel() * t.element_size(), sp),
+                    "download")
         stream.synchronize()
 
     e2e_step()

@@ -367,6 +367,15 @@ int tecto_batch_step(tecto_batch *batch, int nSteps, tecto_stream_t stream);
 int tecto_batch_size(const tecto_batch *batch, int *worlds, size_t *cells);
 int tecto_batch_launch_count(const tecto_batch *batch, uint64_t *count);
 int tecto_batch_check(tecto_batch *batch, tecto_stream_t stream);
+/* One field of every member world to or from one packed host buffer, stream-ordered like
+ * tecto_world_upload_async: member order (the order of tecto_batch_add, removed worlds taken out),
+ * each world's W*H elements, bytes = the batch's cells x the element size (fields HEIGHT, WATER,
+ * SEDIMENT, FLUX, PLATE_ID, LABELS).  One host<->device copy through a staging buffer the batch
+ * keeps, and one device scatter or gather, instead of one copy per world. */
+int tecto_batch_upload_async(tecto_batch *batch, int field, const void *host, size_t bytes, tecto_stream_t stream);
+int tecto_batch_download_async(tecto_batch *batch, int field, void *host, size_t bytes, tecto_stream_t stream);
+/* The first cell of each member in that packing, and the total (capacity >= worlds + 1). */
+int tecto_batch_offsets(const tecto_batch *batch, size_t *cell_offsets, int capacity);
 /* Phases over every world of the batch (one launch per sub-iteration): for measurement and
  * parity tests, like the per-world phase calls above. */
 int tecto_batch_phase_hydraulic(tecto_batch *batch, int iterations, float dt, tecto_stream_t stream);

@@ -268,6 +268,9 @@ def _declare(L: C.CDLL) -> None:
         "tecto_batch_check": ([P, P], C.c_int),
         "tecto_batch_phase_hydraulic": ([P, C.c_int, C.c_float, P], C.c_int),
         "tecto_batch_phase_thermal": ([P, C.c_int, P], C.c_int),
+        "tecto_batch_upload_async": ([P, C.c_int, P, C.c_size_t, P], C.c_int),
+        "tecto_batch_download_async": ([P, C.c_int, P, C.c_size_t, P], C.c_int),
+        "tecto_batch_offsets": ([P, C.POINTER(C.c_size_t), C.c_int], C.c_int),
         "tecto_autotune": ([C.POINTER(Settings), P, P, C.c_int, P, C.POINTER(Tuning)], C.c_int),
         "tecto_batch_autotune": ([P, P, C.POINTER(Tuning)], C.c_int),
         "tecto_world_autotune": ([P, P, C.POINTER(Tuning)], C.c_int),
@@ -620,6 +623,21 @@ class Batch:
 
     def thermal(self, iters: int, stream=None) -> None:
         check(lib().tecto_batch_phase_thermal(self.ptr, iters, _stream(stream)), "tecto_batch_phase_thermal")
+
+    def offsets(self) -> np.ndarray:
+        """First cell of each member in the packed layout, then the total."""
+        n, _ = self.size()
+        out = (C.c_size_t * (n + 1))()
+        check(lib().tecto_batch_offsets(self.ptr, out, n + 1), "tecto_batch_offsets")
+        return np.array(out[:], np.int64)
+
+    def upload_packed_async(self, field: int, host_ptr: int, nbytes: int, stream=None) -> None:
+        check(lib().tecto_batch_upload_async(self.ptr, field, host_ptr, nbytes, _stream(stream)),
+              "tecto_batch_upload_async")
+
+    def download_packed_async(self, field: int, host_ptr: int, nbytes: int, stream=None) -> None:
+        check(lib().tecto_batch_download_async(self.ptr, field, host_ptr, nbytes, _stream(stream)),
+              "tecto_batch_download_async")
 
     def autotune(self, stream=None) -> Tuning:
         t = Tuning()

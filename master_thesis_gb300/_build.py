@@ -33,6 +33,7 @@ SOURCES = [
     "k_ccl.cu",
     "tecto_export.cu",
     "tecto_init.cu",
+    "tecto_packed.cu",
     "settings.cpp",
 ]
 

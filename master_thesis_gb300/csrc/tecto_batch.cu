@@ -109,8 +109,11 @@ void batch_release(Batch &b)
     uplift_ref_release(b);
     if (b.table_arena) cudaFree(b.table_arena);
     if (b.arena) cudaFree(b.arena);
+    if (b.stage) cudaFree(b.stage);
     b.table_arena = nullptr;
     b.arena = nullptr;
+    b.stage = nullptr;
+    b.stage_bytes = 0;
     b.capacity = 0;
     b.arena_bytes = 0;
     b.table_bytes = 0;

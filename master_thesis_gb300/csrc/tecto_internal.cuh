@@ -193,6 +193,8 @@ struct Batch {
     SortScratch sort{};
     UpliftRefScratch upref{};
     int upref_final = 0;                     // jfa[] half holding the last step's seeds
+    void *stage = nullptr;                   // packed host transfers: one field of every member
+    size_t stage_bytes = 0;
     // graphs of one step keyed by (cur_h, cur_wsf, cur_id, ccl)
     cudaGraphExec_t graphs[16] = {};
     bool graph_valid[16] = {};

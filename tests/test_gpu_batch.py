@@ -156,3 +156,48 @@ def test_async_field_copies_round_trip(stream):
     np.testing.assert_array_equal(out.numpy(), b.download(T.FIELD_WATER))
     with pytest.raises(T.TectoError):
         T.check(L.tecto_world_upload_async(a.ptr, T.FIELD_WATER, water.data_ptr(), 12, sp), "upload_async")
+
+
+def test_packed_transfers_equal_per_world_copies(stream):
+    """tecto_batch_upload_async / download_async: one packed host buffer per field for all worlds
+    gives the same state as copies world by world."""
+    torch = pytest.importorskip("torch")
+    s = settings()
+    a = [make(sp, s) for sp in SPECS]
+    b = [make(sp, s) for sp in SPECS]
+    ba, bb = T.Batch(), T.Batch()
+    for w in a:
+        ba.add(w, stream)
+    for w in b:
+        bb.add(w, stream)
+    ba.step(2, stream)
+    bb.step(2, stream)
+    stream.synchronize()
+    rng = np.random.default_rng(9)
+    offs = bb.offsets()
+    assert offs[-1] == sum(w.W * w.H for w in b)
+    fields = {T.FIELD_HEIGHT: np.float32, T.FIELD_WATER: np.float32, T.FIELD_SEDIMENT: np.float32,
+              T.FIELD_FLUX: np.float32, T.FIELD_PLATE_ID: np.uint8}
+    for f, dt in fields.items():
+        per = [(rng.random(w.download(f).shape) * 3).astype(dt) for w in a]
+        for w, v in zip(a, per):
+            w.upload(f, v, stream)
+        packed = torch.from_numpy(np.concatenate([v.ravel() for v in per])).pin_memory()
+        bb.upload_packed_async(f, packed.data_ptr(), packed.numel() * packed.element_size(), stream)
+    stream.synchronize()
+    ba.step(3, stream)
+    bb.step(3, stream)
+    for f in (T.FIELD_HEIGHT, T.FIELD_WATER, T.FIELD_FLUX, T.FIELD_PLATE_ID, T.FIELD_LABELS):
+        out = torch.empty(int(offs[-1]) * (16 if f == T.FIELD_FLUX else 1 if f == T.FIELD_PLATE_ID else 4),
+                          dtype=torch.uint8).pin_memory()
+        bb.download_packed_async(f, out.data_ptr(), out.numel(), stream)
+        stream.synchronize()
+        got = out.numpy()
+        for i, w in enumerate(a):
+            ref = w.download(f).ravel().view(np.uint8)
+            esz = ref.size // (w.W * w.H)
+            np.testing.assert_array_equal(got[offs[i] * esz: offs[i + 1] * esz], ref, err_msg=f"world {i} field {f}")
+    with pytest.raises(T.TectoError):
+        bb.upload_packed_async(T.FIELD_HEIGHT, packed.data_ptr(), 12, stream)
+    ba.close()
+    bb.close()
