@@ -499,6 +499,18 @@ def engine_extras(args, T, torch, stream, s, specs, total, batched_value):
     out["plate_dynamics_2048"] = {"ms_per_step": msd, "ms_per_step_without": ms2048,
                                   "overhead_frac": msd / ms2048 - 1.0,
                                   "workload": "one 2048x2048 world, 32 plates, plate dynamics on"}
+    sp = T.baseline_settings()
+    sp.step.plateDynamics = T.PLATE_DYNAMICS_REFERENCE
+    sp.step.platePolicy = T.PLATE_RELABEL | T.PLATE_MERGE
+    sp.sim.iterationsForCCL = 1
+    _, msp = plain_world_rate(T, torch, stream, 2048, 2048, 32, 1.0, 20, sp)
+    sc = T.baseline_settings()
+    sc.sim.iterationsForCCL = 1
+    _, msc = plain_world_rate(T, torch, stream, 2048, 2048, 32, 1.0, 20, sc)
+    out["plate_policy_2048"] = {"ms_per_step": msp, "ms_per_step_ccl_every_step": msc,
+                                "overhead_frac": msp / msc - 1.0,
+                                "workload": "one 2048x2048 world, 32 plates, plate dynamics, relabel after a CCL "
+                                            "on every step, merges; compared with the same CCL cadence alone"}
     si = T.default_settings()  # the reference's defaults: 16 plates, Voronoi generations of 200 and 500 seeds
     w = T.World(si, 2048, 2048, seed=1000)
     w.init_reference(stream)
@@ -563,6 +575,7 @@ def run_case(args):
     """Small fixed workloads for ncu captures (no timing, no JSON line):
     erosion2048  one 5-iteration thermal launch and one fused hydraulic launch on a 2048^2 world;
     plain2048    4 steps of one 2048^2 world, 32 plates;
+    policy2048   the same with plate dynamics, relabel after a CCL on every step, and merges;
     batch        the mixed-size batch with the default tile and digit width, 4 steps."""
     import torch
 
@@ -578,6 +591,14 @@ def run_case(args):
         w.upload(T.FIELD_SEDIMENT, np.abs(rng.normal(0, 0.01, (2048, 2048))).astype(np.float32))
         w.thermal(5, stream)
         w.hydraulic(1, s.step.hydraulicDt, stream)
+        w.check(stream)
+    elif args.case == "policy2048":
+        s.step.plateDynamics = T.PLATE_DYNAMICS_REFERENCE
+        s.step.platePolicy = T.PLATE_RELABEL | T.PLATE_MERGE
+        s.sim.iterationsForCCL = 1
+        w = T.World(s, 2048, 2048, seed=1000)
+        w.init_synthetic_device(32, 1.0, 1)
+        w.step(4, stream)
         w.check(stream)
     elif args.case == "plain2048":
         w = T.World(s, 2048, 2048, seed=1000)
@@ -608,7 +629,8 @@ def main():
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
     ap.add_argument("--serve-requests", type=int, default=64)
     ap.add_argument("--quick", action="store_true", help="headline only (no plain/served/large-world lines)")
-    ap.add_argument("--case", choices=["erosion2048", "plain2048", "batch"], help="a small fixed workload for profilers")
+    ap.add_argument("--case", choices=["erosion2048", "plain2048", "policy2048", "batch"],
+                    help="a small fixed workload for profilers")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_setup()

@@ -17,7 +17,7 @@ namespace tecto {
 namespace {
 
 // Per-plate mass and size over all cells, and the angular sums of every cell whose x and y are
-// multiples of 10, over 256 x 64 tiles of the batch.  Each thread walks one column of its tile and
+// multiples of 10, over 256 x 16 tiles of the batch.  Each thread walks one column of its tile and
 // keeps a run of equal plate ids in registers; runs and samples go to shared sums, the block's
 // sums to the world's PlateAcc.
 __global__ __launch_bounds__(256) void k_plate_stats(const WorldDev *worlds, const uint2 *tiles, int cur_h,

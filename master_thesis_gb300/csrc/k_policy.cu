@@ -31,8 +31,8 @@ __device__ __forceinline__ bool relabel_due(const WorldDev &wd, int period)
     return period == 0 || wd.ctl->iteration % (uint32_t)period == 0u;
 }
 
-// Component sizes: clear, then count the cells of each label.  Grid: TK_STATS tiles, one column of
-// 64 cells per thread.
+// Component sizes: clear, then count the cells of each label; then the roots' keys; then the ids.
+// Grid: TK_STATS tiles, one column of a tile per thread.
 template <int PHASE>
 __global__ __launch_bounds__(256) void k_rl_cells(const WorldDev *worlds, const uint2 *tiles, int cur_id,
                                                   int period)
@@ -48,12 +48,25 @@ __global__ __launch_bounds__(256) void k_rl_cells(const WorldDev *worlds, const 
     uint32_t *lookup = reinterpret_cast<uint32_t *>(wd.s1);
     unsigned long long *keys = reinterpret_cast<unsigned long long *>(wd.vel);
     uint8_t *id = wd.id[cur_id];
+    if (PHASE == 1) {
+        // cells down a column mostly share a label: count runs in a register, one atomic per run
+        uint32_t run = 0xffffffffu, n = 0u;
+        for (int y = y0; y < y1; ++y) {
+            const uint32_t lab = wd.labels[(uint32_t)y * (uint32_t)wd.W + (uint32_t)x];
+            if (lab != run) {
+                if (n) atomicAdd(count + run, n);
+                run = lab;
+                n = 0u;
+            }
+            ++n;
+        }
+        if (n) atomicAdd(count + run, n);
+        return;
+    }
     for (int y = y0; y < y1; ++y) {
         const uint32_t i = (uint32_t)y * (uint32_t)wd.W + (uint32_t)x;
         if (PHASE == 0) {
             count[i] = 0u;
-        } else if (PHASE == 1) {
-            atomicAdd(count + wd.labels[i], 1u);
         } else if (PHASE == 2) {
             // roots: one key per component, the plate's largest component, a cleared lookup entry
             if (wd.labels[i] == i) {

@@ -91,7 +91,7 @@ constexpr float kMassLimit = 1099511627776.0f;     // |h| clamp before scaling, 
 constexpr float kAngScale = 4294967296.0f;         // 2^32
 constexpr float kFricScale = 1099511627776.0f;     // 2^40
 constexpr float kFricLimit = 4194304.0f;           // |friction term| clamp, 2^22
-constexpr int kStatTileX = 256, kStatTileY = 64;   // TK_STATS tile
+constexpr int kStatTileX = 256, kStatTileY = 16;   // TK_STATS tile
 constexpr float kTwoPiF = 6.28318548202514648f;    // CURAND_2PI as a float
 
 // Per-world state of the plate policy (relabel and merges).
