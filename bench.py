@@ -535,6 +535,21 @@ def engine_extras(args, T, torch, stream, s, specs, total, batched_value):
         w.load_snapshot(os.path.join(d, "w.snap"), stream)
         exp_ms["snapshot_load"] = (time.perf_counter() - t0) * 1e3
     w.close()
+    # the reference's own configuration end to end: its initialisation, its default KernelSettings and
+    # step constants (10 hydraulic sub-iterations at dt 1, one thermal pass), its uplift
+    sr = T.default_settings()
+    sr.step.upliftMode = T.UPLIFT_REFERENCE
+    wr = T.World(sr, 2048, 2048, seed=1000)
+    wr.init_reference(stream)
+    wr.step(3, stream)
+    stream.synchronize()
+    msr = event_ms(torch, stream, lambda: wr.step(10, stream)) / 10
+    wr.check(stream)
+    wr.close()
+    out["reference_physics_2048"] = {"ms_per_step": msr, "value": 2048 * 2048 / (msr / 1e3),
+                                     "unit": "cell-updates/s",
+                                     "workload": "one 2048x2048 world initialised as the reference does, its default "
+                                                 "settings (split hydraulic path at dt 1), the reference uplift"}
     out["init_reference_2048"] = {"ms": min(init_ms), "workload": "2048x2048, the reference's default settings "
                                   "(16 plates, Voronoi generations of 200 and 500 seeds), wall time incl. host draws"}
     out["output_2048_ms"] = exp_ms
