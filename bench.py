@@ -291,6 +291,27 @@ def plain_world_rate(T, torch, stream, W, H, plates, vel, steps, settings):
     return W * H * steps / (ms / 1e3), ms / steps
 
 
+def rank_worlds(rank):
+    """The worlds one rank steps: replicas run their own mixed batch (a different shape seed per
+    rank); no data crosses ranks."""
+    return mixed_worlds(seed=SHAPE_SEED + rank)
+
+
+def reduce_max(x, dist, device):
+    """x maximised over the ranks (the slowest rank's time), or x alone without a process group."""
+    import torch
+
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(ws, cells_per_rank, steps, ms_max):
+    """Whole-job cell-updates/s: every rank's cells times the steps, over the slowest rank's time."""
+    return ws * cells_per_rank * steps / (ms_max / 1e3)
+
+
 def run_engine(args, ws, rank, local):
     import torch
 
@@ -308,14 +329,11 @@ def run_engine(args, ws, rank, local):
             dist.barrier()
 
     def max_over_ranks(x):
-        t = torch.tensor([x], device="cuda", dtype=torch.float64)
-        if dist is not None:
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return reduce_max(x, dist, "cuda")
 
     stream = torch.cuda.Stream()
     s = T.baseline_settings()  # hydraulicTile = sortRadixBits = 0: the autotuner's choice
-    specs = mixed_worlds(seed=SHAPE_SEED + rank)
+    specs = rank_worlds(rank)
     total = sum(W * H for W, H, *_ in specs)
     tuning = T.autotune(s, [(W, H) for W, H, *_ in specs], stream)
 
@@ -343,7 +361,7 @@ def run_engine(args, ws, rank, local):
     ms = max_over_ranks(e0.elapsed_time(e1))
     launches = batch.launches - launches0
     batch.check(stream)
-    value = ws * total * args.steps / (ms / 1e3)
+    value = job_rate(ws, total, args.steps, ms)
 
     # dominant kernel: the fused hydraulic sub-iteration over the whole batch, on the same stream
     reps = 20
@@ -385,7 +403,7 @@ def run_engine(args, ws, rank, local):
     e2e_ev = event_ms(torch, stream, lambda: [e2e_step() for _ in range(e2e_steps)])
     wall_ms = (time.perf_counter() - t0) * 1e3
     e2e_ms = max_over_ranks(max(e2e_ev, wall_ms))
-    e2e_value = ws * total * e2e_steps / (e2e_ms / 1e3)
+    e2e_value = job_rate(ws, total, e2e_steps, e2e_ms)
     h2d = sum(t.numel() * t.element_size() for hs in hosts for t in hs.values())
     d2h = sum(t.numel() * t.element_size() for os_ in outs for t in os_.values())
     batch.check(stream)

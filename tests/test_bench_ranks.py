@@ -1,0 +1,67 @@
+"""bench.py's multi-rank path on the CPU with two gloo ranks: each rank steps its own replica batch
+(different worlds, no exchange), the timing is the slowest rank's, the job rate aggregates all
+ranks, and the reference arm runs on rank 0 alone."""
+from __future__ import annotations
+
+import os
+import socket
+import sys
+
+import pytest
+import torch.distributed as dist
+import torch.multiprocessing as mp
+
+from conftest import ROOT
+
+
+def free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank(rank, ws, port, out):
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(ws),
+                      LOCAL_RANK=str(rank))
+    assert bench.dist_setup() == (ws, rank, rank)
+    dist.init_process_group("gloo", rank=rank, world_size=ws)
+    try:
+        ms = bench.reduce_max(10.0 * (rank + 1), dist, "cpu")
+        specs = bench.rank_worlds(rank)
+        cells = sum(W * H for W, H, *_ in specs)
+        cell_sums = [0, 0]
+        dist.all_gather_object(cell_sums, cells)
+        dist.barrier()
+        ref = bench.run_reference(None, ws, rank) if rank != 0 else "skipped"
+        out.put((rank, ms, [s[:2] for s in specs[:4]], cell_sums, ref))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_two_gloo_ranks():
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = free_port()
+    procs = [ctx.Process(target=_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    (r0, ms0, shapes0, cells0, _), (r1, ms1, shapes1, cells1, ref1) = res
+    assert ms0 == ms1 == 20.0              # the slowest rank's time on every rank
+    assert shapes0 != shapes1              # replicas: each rank its own worlds
+    assert cells0 == cells1                # every rank saw both totals
+    assert ref1 is None                    # the reference arm: rank 0 alone
+
+
+def test_job_rate_aggregates_ranks():
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    assert bench.job_rate(1, 1000, 4, 2.0) == pytest.approx(2.0e6)
+    assert bench.job_rate(4, 1000, 4, 2.0) == pytest.approx(8.0e6)
