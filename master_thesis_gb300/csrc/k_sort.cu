@@ -21,6 +21,7 @@ namespace tecto {
 namespace {
 
 constexpr int kWarps = kSortThreads / 32;
+constexpr int kLookAhead = 8;  // predecessor tiles read per look-back round
 
 template <int RB>
 struct Digits {
@@ -252,7 +253,9 @@ __global__ __launch_bounds__(kSortThreads) void k_sort_pass(
         carry += tot;
     }
 
-    // Decoupled look-back for the owned digits, walked side by side.
+    // Decoupled look-back for the owned digits, walked side by side.  Each round reads the status
+    // words of up to kLookAhead predecessors at once (independent loads in flight together) and
+    // consumes them newest first until one is not yet published or carries an inclusive prefix.
     uint32_t prefix[DPT];
 #pragma unroll
     for (int c = 0; c < DPT; ++c) prefix[c] = 0;
@@ -268,14 +271,24 @@ __global__ __launch_bounds__(kSortThreads) void k_sort_pass(
 #pragma unroll
             for (int c = 0; c < DPT; ++c) {
                 if (j[c] < 0) continue;
-                const uint32_t s = ld_volatile(status + (size_t)j[c] * R + t + c * kSortThreads);
-                if ((s & ~kValueMask) == 0) {
-                    pending = true;
-                    continue;
+                const uint32_t *col = status + t + c * kSortThreads;
+                const int j0 = j[c];
+                uint32_t sv[kLookAhead];
+#pragma unroll
+                for (int q = 0; q < kLookAhead; ++q) sv[q] = j0 - q >= 0 ? ld_volatile(col + (size_t)(j0 - q) * R) : 0u;
+                int used = 0;
+                bool done = false;
+#pragma unroll
+                for (int q = 0; q < kLookAhead; ++q) {
+                    if (done || used < q || j0 - q < 0) continue;
+                    const uint32_t st = sv[q];
+                    if ((st & ~kValueMask) == 0) continue;  // not yet published: read it again next round
+                    progressed = true;
+                    prefix[c] += st & kValueMask;
+                    used = q + 1;
+                    done = (st & kFlagPrefix) != 0;
                 }
-                progressed = true;
-                prefix[c] += s & kValueMask;
-                j[c] = (s & kFlagPrefix) ? -1 : j[c] - 1;
+                j[c] = done ? -1 : j0 - used;
                 if (j[c] >= 0) pending = true;
             }
             if (pending && !progressed && ++spins > kSpinLimit) {  // a predecessor never published
