@@ -20,7 +20,7 @@ and sort digit width picked by the autotuner.  Beside it:
   plain_2048   one 2048^2 world, 32 plates (plain path; its k_hydro roofline);
   plain_8192   one 8192^2 world, 64 plates, velocities in [-2, 2], 8-connected CCL every step.
 `e2e` repeats the headline through the C ABI with host buffers (packed: one buffer per field for all
-worlds, tecto_batch_upload_async / download_async): every step uploads each world's
+worlds; copies on a second stream overlap the previous or next step's compute): every step uploads each world's
 state from pinned host memory, steps the batch, downloads heights and plate ids, and waits for them.
 Reference arm: the reference path's CPU implementation (the oracle's C restatement, all host
 threads) on a bounded sample of the same mixed-size workload.  With N > 1 (torchrun) every rank
@@ -382,27 +382,39 @@ def run_engine(args, ws, rank, local):
               for f in up_fields}]
     outs = [{f: torch.empty_like(hosts[0][f]).pin_memory() for f in down_fields}]
 
-    def e2e_step():
-        # stream-ordered packed copies from / to pinned host buffers (one copy and one device
-        # scatter / gather per field for all worlds), one wait per step
-        for f, t in hosts[0].items():
-            T.check(L.tecto_batch_upload_async(batch.ptr, f, t.data_ptr(), t.numel() * t.element_size(), sp),
-                    "upload")
-        batch.step(1, stream)
-        for f, t in outs[0].items():
-            T.check(L.tecto_batch_download_async(batch.ptr, f, t.data_ptr(), t.numel() * t.element_size(), sp),
-                    "download")
-        stream.synchronize()
+    copy = torch.cuda.Stream()
+    cs = copy.cuda_stream
 
-    e2e_step()
-    stream.synchronize()
-    e2e_steps = 3
+    def e2e_run(nsteps):
+        # every step: its inputs copied up (one packed buffer per field, staged on a copy stream while
+        # the previous step computes, then scattered into the worlds), the step, its results gathered
+        # and copied down on the copy stream while the next step computes
+        def stage():
+            for f, t in hosts[0].items():
+                T.check(L.tecto_batch_stage_upload_async(batch.ptr, f, t.data_ptr(), t.numel() * t.element_size(),
+                                                         cs), "stage")
+        stage()
+        for k in range(nsteps):
+            for f in hosts[0]:
+                T.check(L.tecto_batch_commit_upload(batch.ptr, f, sp), "commit")
+            if k + 1 < nsteps:
+                stage()
+            batch.step(1, stream)
+            for f, t in outs[0].items():
+                T.check(L.tecto_batch_gather_download(batch.ptr, f, sp), "gather")
+                T.check(L.tecto_batch_fetch_download_async(batch.ptr, f, t.data_ptr(), t.numel() * t.element_size(),
+                                                           cs), "fetch")
+        stream.synchronize()
+        copy.synchronize()
+
+    e2e_run(2)
+    e2e_steps = 4
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    e2e_ev = event_ms(torch, stream, lambda: [e2e_step() for _ in range(e2e_steps)])
+    e2e_run(e2e_steps)
     wall_ms = (time.perf_counter() - t0) * 1e3
-    e2e_ms = max_over_ranks(max(e2e_ev, wall_ms))
+    e2e_ms = max_over_ranks(wall_ms)
     e2e_value = job_rate(ws, total, e2e_steps, e2e_ms)
     h2d = sum(t.numel() * t.element_size() for hs in hosts for t in hs.values())
     d2h = sum(t.numel() * t.element_size() for os_ in outs for t in os_.values())

@@ -374,6 +374,18 @@ int tecto_batch_check(tecto_batch *batch, tecto_stream_t stream);
  * keeps, and one device scatter or gather, instead of one copy per world. */
 int tecto_batch_upload_async(tecto_batch *batch, int field, const void *host, size_t bytes, tecto_stream_t stream);
 int tecto_batch_download_async(tecto_batch *batch, int field, void *host, size_t bytes, tecto_stream_t stream);
+/* The same split in two so that copies overlap compute: stage_upload copies a packed field into a
+ * staging buffer of the batch on copy_stream, commit_upload scatters it into the worlds on the
+ * compute stream (after the copy); gather_download collects a field on the compute stream,
+ * fetch_download copies it to the host on copy_stream (after the gather).  Events inside the batch
+ * order the two streams: a stage waits for the previous commit of that field, a gather for the
+ * previous fetch.  The host buffers must stay valid until copy_stream has passed the copy. */
+int tecto_batch_stage_upload_async(tecto_batch *batch, int field, const void *host, size_t bytes,
+                                   tecto_stream_t copy_stream);
+int tecto_batch_commit_upload(tecto_batch *batch, int field, tecto_stream_t stream);
+int tecto_batch_gather_download(tecto_batch *batch, int field, tecto_stream_t stream);
+int tecto_batch_fetch_download_async(tecto_batch *batch, int field, void *host, size_t bytes,
+                                     tecto_stream_t copy_stream);
 /* The first cell of each member in that packing, and the total (capacity >= worlds + 1). */
 int tecto_batch_offsets(const tecto_batch *batch, size_t *cell_offsets, int capacity);
 /* Phases over every world of the batch (one launch per sub-iteration): for measurement and

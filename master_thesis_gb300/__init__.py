@@ -271,6 +271,10 @@ def _declare(L: C.CDLL) -> None:
         "tecto_batch_upload_async": ([P, C.c_int, P, C.c_size_t, P], C.c_int),
         "tecto_batch_download_async": ([P, C.c_int, P, C.c_size_t, P], C.c_int),
         "tecto_batch_offsets": ([P, C.POINTER(C.c_size_t), C.c_int], C.c_int),
+        "tecto_batch_stage_upload_async": ([P, C.c_int, P, C.c_size_t, P], C.c_int),
+        "tecto_batch_commit_upload": ([P, C.c_int, P], C.c_int),
+        "tecto_batch_gather_download": ([P, C.c_int, P], C.c_int),
+        "tecto_batch_fetch_download_async": ([P, C.c_int, P, C.c_size_t, P], C.c_int),
         "tecto_autotune": ([C.POINTER(Settings), P, P, C.c_int, P, C.POINTER(Tuning)], C.c_int),
         "tecto_batch_autotune": ([P, P, C.POINTER(Tuning)], C.c_int),
         "tecto_world_autotune": ([P, P, C.POINTER(Tuning)], C.c_int),

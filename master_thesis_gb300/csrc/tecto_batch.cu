@@ -110,6 +110,17 @@ void batch_release(Batch &b)
     if (b.table_arena) cudaFree(b.table_arena);
     if (b.arena) cudaFree(b.arena);
     if (b.stage) cudaFree(b.stage);
+    for (int f = 0; f < 6; ++f) {
+        if (b.up_stage[f]) cudaFree(b.up_stage[f]);
+        if (b.down_stage[f]) cudaFree(b.down_stage[f]);
+        b.up_stage[f] = b.down_stage[f] = nullptr;
+        b.up_bytes[f] = b.down_bytes[f] = 0;
+        cudaEvent_t *evs[4] = {&b.ev_up_ready[f], &b.ev_up_free[f], &b.ev_down_ready[f], &b.ev_down_free[f]};
+        for (cudaEvent_t *e : evs) {
+            if (*e) cudaEventDestroy(*e);
+            *e = nullptr;
+        }
+    }
     b.table_arena = nullptr;
     b.arena = nullptr;
     b.stage = nullptr;

@@ -201,3 +201,49 @@ def test_packed_transfers_equal_per_world_copies(stream):
         bb.upload_packed_async(T.FIELD_HEIGHT, packed.data_ptr(), 12, stream)
     ba.close()
     bb.close()
+
+
+def test_pipelined_transfers_equal_plain_ones(stream):
+    """Staged uploads and gathered downloads on a second stream (tecto_batch_stage_upload_async /
+    commit_upload / gather_download / fetch_download_async) give the same worlds and results as
+    the single-stream packed calls, step after step with new inputs each step."""
+    torch = pytest.importorskip("torch")
+    s = settings()
+    a = [make(sp, s) for sp in SPECS]
+    b = [make(sp, s) for sp in SPECS]
+    ba, bb = T.Batch(), T.Batch()
+    for w in a:
+        ba.add(w, stream)
+    for w in b:
+        bb.add(w, stream)
+    L = T.lib()
+    copy = torch.cuda.Stream()
+    cs, ss = copy.cuda_stream, stream.cuda_stream
+    total = int(bb.offsets()[-1])
+    rng = np.random.default_rng(4)
+    inputs = [torch.from_numpy((rng.random(total) * 2).astype(np.float32)).pin_memory() for _ in range(3)]
+    outs_a = [torch.empty(total, dtype=torch.float32).pin_memory() for _ in range(3)]
+    outs_b = [torch.empty(total, dtype=torch.float32).pin_memory() for _ in range(3)]
+    nb = total * 4
+    T.check(L.tecto_batch_stage_upload_async(bb.ptr, T.FIELD_WATER, inputs[0].data_ptr(), nb, cs), "stage")
+    for k in range(3):
+        # plain packed path
+        ba.upload_packed_async(T.FIELD_WATER, inputs[k].data_ptr(), nb, stream)
+        ba.step(1, stream)
+        ba.download_packed_async(T.FIELD_HEIGHT, outs_a[k].data_ptr(), nb, stream)
+        # pipelined path: the next step's input is staged while this step runs
+        T.check(L.tecto_batch_commit_upload(bb.ptr, T.FIELD_WATER, ss), "commit")
+        if k + 1 < 3:
+            T.check(L.tecto_batch_stage_upload_async(bb.ptr, T.FIELD_WATER, inputs[k + 1].data_ptr(), nb, cs),
+                    "stage")
+        bb.step(1, stream)
+        T.check(L.tecto_batch_gather_download(bb.ptr, T.FIELD_HEIGHT, ss), "gather")
+        T.check(L.tecto_batch_fetch_download_async(bb.ptr, T.FIELD_HEIGHT, outs_b[k].data_ptr(), nb, cs), "fetch")
+    stream.synchronize()
+    copy.synchronize()
+    for k in range(3):
+        np.testing.assert_array_equal(outs_a[k].numpy(), outs_b[k].numpy(), err_msg=f"step {k}")
+    for wa, wb in zip(a, b):
+        np.testing.assert_array_equal(wa.download(T.FIELD_WATER), wb.download(T.FIELD_WATER))
+    ba.close()
+    bb.close()
