@@ -4,6 +4,7 @@ from __future__ import annotations
 import math
 
 import numpy as np
+import pytest
 
 import master_thesis_gb300 as T
 import oracle as O
@@ -49,3 +50,34 @@ def test_thermal_conserves_mass_roughly():
     h, _, _ = T.generate_world(48, 40, 6, 1.0, 4)
     out = O.thermal(h, 10, T.baseline_settings())
     assert abs(float(out.astype(np.float64).sum() - h.astype(np.float64).sum())) < 1e-3
+
+
+@pytest.mark.parametrize("sigma,radius", [(1.5, 3), (0.8, 1), (3.0, 8)])
+def test_gaussian_uplift_against_numpy_convolution(sigma, radius):
+    """The new Gaussian uplift (upliftAmount on convergent cells, separable blur with wrap) against an
+    independent float64 restatement with numpy: the oracle's resolve with and without the uplift
+    differs by the blurred field, to float32 rounding."""
+    import master_thesis_gb300 as T
+    W, H = 48, 40
+    h, ids, pl = T.generate_world(W, H, 7, 1.8, 12)
+    offx, offy, _ = O.plate_offsets(pl)
+    _, word, _, _ = O.collision_words(ids, offx, offy)
+    s = T.baseline_settings()
+    s.step.upliftSigma, s.step.upliftRadius, s.step.upliftAmount = sigma, radius, 0.25
+    bm = np.zeros(32385, np.uint8)
+    div = np.zeros(1013, np.uint32)
+    s.step.upliftMode = T.UPLIFT_GAUSSIAN
+    hg, *_ = O.resolve(ids, h, word, offx, offy, bm, div, s, 1000, 0)
+    s.step.upliftMode = T.UPLIFT_NONE
+    hn, *_ = O.resolve(ids, h, word, offx, offy, bm, div, s, 1000, 0)
+    conv = (word > 0xFF).astype(np.float64) * 0.25
+    k = np.exp(-0.5 * (np.arange(-radius, radius + 1) / sigma) ** 2)
+    k /= k.sum()
+    blur = np.zeros_like(conv)
+    for d, wgt in zip(range(-radius, radius + 1), k):
+        blur += wgt * np.roll(conv, -d, axis=1)
+    out = np.zeros_like(conv)
+    for d, wgt in zip(range(-radius, radius + 1), k):
+        out += wgt * np.roll(blur, -d, axis=0)
+    assert (word > 0xFF).sum() > 10
+    np.testing.assert_allclose(hg.astype(np.float64) - hn.astype(np.float64), out, atol=2e-6, rtol=0)
