@@ -101,3 +101,40 @@ def test_unknown_policy_bits_are_refused(stream):
     w.init_synthetic(3, 1.0, 1, stream)
     with pytest.raises(T.TectoError):
         w.step(1, stream)
+
+
+def test_reference_configuration_100_steps(stream):
+    """Everything on for 100 steps: the reference's initialisation, default settings and uplift,
+    plate dynamics with an asthenosphere texture, relabel after every CCL, merges.  The engine
+    stays bit-identical to the oracle throughout."""
+    s = T.default_settings()
+    s.step.upliftMode = T.UPLIFT_REFERENCE
+    s.step.hydraulicIterations = 4
+    s.step.plateDynamics = T.PLATE_DYNAMICS_REFERENCE
+    s.step.platePolicy = T.PLATE_RELABEL | T.PLATE_MERGE
+    s.sim.iterationsForCCL = 5
+    s.sim.numStartingPlates = 10
+    s.sim.numVoronoiSeeds[0], s.sim.numVoronoiSeeds[1] = 60, 150
+    s.kernel.minPlateSize = 20
+    s.kernel.targetMaximumPlateArea = 6000
+    W, H = 128, 96
+    w = T.World(s, W, H, seed=2024)
+    w.init_reference(stream)
+    pr = np.random.default_rng(2).random((40, 50)).astype(np.float32)
+    w.set_asthenosphere(pr, stream)
+    o = O.OracleWorld(s, w.download(T.FIELD_HEIGHT, stream), w.download(T.FIELD_PLATE_ID, stream),
+                      w.plates(stream), 2024)
+    o.dyn = w.plate_dynamics(stream)
+    o.pressure = pr
+    counts = []
+    for chunk in range(10):
+        w.step(10, stream)
+        o.step(10)
+        w.check(stream)
+        for f in FIELDS:
+            np.testing.assert_array_equal(w.download(f, stream), oracle_field(o, f), err_msg=f"step {10 * chunk + 9} field {f}")
+        np.testing.assert_array_equal(w.plates(stream), o.plates)
+        np.testing.assert_array_equal(w.plate_dynamics(stream), o.dyn)
+        counts.append(len(np.unique(o.id)))
+    assert w.iteration == 100
+    assert min(counts) >= 1
