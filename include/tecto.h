@@ -502,6 +502,10 @@ int tecto_server_set_dry_cost(tecto_server *server, double seconds_per_mcell_ste
  * Everything else starts at zero, iteration 0.  Plate fragments keep their id (the reference's
  * post-CCL relabel is not part of this engine). */
 int tecto_world_init_reference(tecto_world *world, tecto_stream_t stream);
+/* PlateTectonicSim::initialize(numStartingPlates, numVoronoiSeeds) with its arguments: stores them in
+ * the world's settings and runs tecto_world_init_reference. */
+int tecto_world_init(tecto_world *world, int numPlates, const int *numVoronoiSeeds, int generations,
+                     tecto_stream_t stream);
 /* The host part alone: seed_x / seed_y / seed_id (capacity entries; *count = seeds of the last
  * generation, or the plate centres) and the plate records it draws. */
 int tecto_reference_seeds(int width, int height, uint32_t seed, int numPlates, const int *numVoronoiSeeds,

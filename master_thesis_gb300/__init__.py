@@ -256,6 +256,7 @@ def _declare(L: C.CDLL) -> None:
         "tecto_world_bytes": ([C.c_int, C.c_int], C.c_size_t),
         "tecto_world_init_synthetic_device": ([P, C.c_int, C.c_float, C.c_uint64, P], C.c_int),
         "tecto_world_init_reference": ([P, P], C.c_int),
+        "tecto_world_init": ([P, C.c_int, P, C.c_int, P], C.c_int),
         "tecto_reference_seeds": ([C.c_int, C.c_int, C.c_uint32, C.c_int, P, C.c_int, P, P, P, C.c_int,
                                    C.POINTER(C.c_int), P, P], C.c_int),
         "tecto_batch_create": ([C.POINTER(P)], C.c_int),

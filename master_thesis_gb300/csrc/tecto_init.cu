@@ -148,6 +148,23 @@ using namespace tecto;
 
 extern "C" {
 
+int tecto_world_init(tecto_world *world, int numPlates, const int *numVoronoiSeeds, int generations,
+                     tecto_stream_t stream)
+{
+    if (!world || numPlates < 1 || numPlates > kPlates || generations < 0 || generations > TECTO_MAX_VORONOI_GENS ||
+        (generations > 0 && !numVoronoiSeeds)) {
+        set_error("tecto_world_init: 1..255 plates, 0..8 Voronoi generations");
+        return TECTO_ERR_INVALID;
+    }
+    tecto_settings s = world->settings;
+    s.sim.numStartingPlates = numPlates;
+    s.sim.numVoronoiGenerations = generations;
+    for (int g = 0; g < generations; ++g) s.sim.numVoronoiSeeds[g] = numVoronoiSeeds[g];
+    const int rc = tecto_world_set_settings(world, &s);
+    if (rc != TECTO_OK) return rc;
+    return tecto_world_init_reference(world, stream);
+}
+
 int tecto_reference_seeds(int width, int height, uint32_t seed, int numPlates, const int *numVoronoiSeeds,
                           int generations, float *seed_x, float *seed_y, uint8_t *seed_id, int capacity,
                           int *count, tecto_plate *plates, tecto_plate_dynamics *dynamics)

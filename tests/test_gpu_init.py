@@ -85,3 +85,23 @@ def test_server_admits_reference_initialised_worlds(stream):
         w.step(q.steps, stream)
         assert np.float32(w.download(T.FIELD_HEIGHT, stream).astype(np.float64).sum()) == res[i].height_checksum
     sv.close()
+
+
+def test_initialize_with_arguments(stream):
+    """tecto_world_init(world, plates, generations): initialize(numStartingPlates, numVoronoiSeeds)."""
+    import ctypes as C
+    s = T.default_settings()
+    a = T.World(s, 80, 60, seed=11)
+    b = T.World(s, 80, 60, seed=11)
+    gens = (C.c_int * 2)(30, 70)
+    T.check(T.lib().tecto_world_init(a.ptr, 6, gens, 2, stream.cuda_stream), "tecto_world_init")
+    s2 = s.copy()
+    s2.sim.numStartingPlates, s2.sim.numVoronoiGenerations = 6, 2
+    s2.sim.numVoronoiSeeds[0], s2.sim.numVoronoiSeeds[1] = 30, 70
+    b.set_settings(s2)
+    b.init_reference(stream)
+    for f in (T.FIELD_HEIGHT, T.FIELD_PLATE_ID, T.FIELD_LABELS):
+        np.testing.assert_array_equal(a.download(f, stream), b.download(f, stream))
+    np.testing.assert_array_equal(a.plates(stream), b.plates(stream))
+    with pytest.raises(T.TectoError):
+        T.check(T.lib().tecto_world_init(a.ptr, 0, gens, 2, stream.cuda_stream), "tecto_world_init")
