@@ -493,6 +493,28 @@ int tecto_server_set_init(tecto_server *server, int mode);
 /* Dry-run cost model: seconds one tick takes per million active cells (default 2e-4). */
 int tecto_server_set_dry_cost(tecto_server *server, double seconds_per_mcell_step);
 
+/* ---- live serving: requests submitted as they come, the caller drives the ticks ----------
+ *
+ * tecto_server_submit queues a copy of *request and returns its ticket (0, 1, 2, ... in submission
+ * order); the request's arrival_s is replaced by the submission time on the server's clock (seconds
+ * since tecto_server_create; the simulated clock in a dry run).  A request that can never be served
+ * (invalid, or larger than the whole budget) is done at once with TECTO_ERR_INVALID or
+ * TECTO_ERR_BUDGET as its status.  tecto_server_tick admits waiting requests first-come first-served
+ * against the budget, advances every admitted world one step as one batch, and retires the worlds
+ * that are done (checksum, and the outputs of tecto_server_set_output named request_<ticket>);
+ * with nothing admitted it does no device work.  It reports the admitted and waiting counts after
+ * the tick.  If a tick fails, every pending request takes its error as status and leaves.
+ * tecto_server_poll gives a ticket's state and result; tecto_server_live_stats summarises the
+ * submitted requests (wall_s = the server clock now).  One host thread owns a server;
+ * tecto_server_run_trace is refused while live requests are pending. */
+#define TECTO_REQUEST_WAITING 0
+#define TECTO_REQUEST_RUNNING 1
+#define TECTO_REQUEST_DONE 2
+int tecto_server_submit(tecto_server *server, const tecto_request *request, int *ticket);
+int tecto_server_tick(tecto_server *server, tecto_stream_t stream, int *active, int *waiting);
+int tecto_server_poll(tecto_server *server, int ticket, int *state, tecto_request_result *result);
+int tecto_server_live_stats(tecto_server *server, tecto_server_stats *stats);
+
 /* The reference's world initialisation (PlateTectonicSim::initializeTectonics,
  * plate_tectonic_sim.cu:705-773) from the world's settings (sim.numStartingPlates,
  * sim.numVoronoiSeeds[0..numVoronoiGenerations)) and its seed: plate centres, Voronoi seed

@@ -39,6 +39,7 @@ PNG_GRAY16, PNG_RGB8, PNG_GRAY8 = 0, 1, 2
 EXPORT_HEIGHT_GRAY16, EXPORT_PLATES_RGB = 0, 1
 SERVER_OUT_HEIGHT_PNG, SERVER_OUT_PLATES_PNG, SERVER_OUT_SNAPSHOT = 1, 2, 4
 SERVER_INIT_SYNTHETIC, SERVER_INIT_REFERENCE = 0, 1
+REQUEST_WAITING, REQUEST_RUNNING, REQUEST_DONE = 0, 1, 2
 
 (FIELD_HEIGHT, FIELD_WATER, FIELD_SEDIMENT, FIELD_FLUX, FIELD_PLATE_ID, FIELD_LABELS,
  FIELD_COLLISION, FIELD_TYPE_BITMAP, FIELD_DIV_BITMAP, FIELD_SORT_KEYS, FIELD_SORT_VALS,
@@ -292,6 +293,10 @@ def _declare(L: C.CDLL) -> None:
         "tecto_server_set_dry_cost": ([P, C.c_double], C.c_int),
         "tecto_server_set_init": ([P, C.c_int], C.c_int),
         "tecto_server_set_output": ([P, C.c_char_p, C.c_int, C.c_float, C.c_float], C.c_int),
+        "tecto_server_submit": ([P, C.POINTER(Request), C.POINTER(C.c_int)], C.c_int),
+        "tecto_server_tick": ([P, P, C.POINTER(C.c_int), C.POINTER(C.c_int)], C.c_int),
+        "tecto_server_poll": ([P, C.c_int, C.POINTER(C.c_int), C.POINTER(RequestResult)], C.c_int),
+        "tecto_server_live_stats": ([P, C.POINTER(ServerStats)], C.c_int),
         "tecto_selftest_div": ([P, P, P, C.c_size_t, P], C.c_int),
         "tecto_png_encode": ([P, C.c_int, C.c_int, C.c_int, P, C.c_size_t, C.POINTER(C.c_size_t)], C.c_int),
         "tecto_plate_palette": ([P], C.c_int),
@@ -725,6 +730,40 @@ class Server:
 
     def run_trace_sequential(self, requests, stream=None):
         return self._run(lib().tecto_server_run_trace_sequential, requests, stream)
+
+    # live serving: submit as requests come, drive the ticks, poll for results
+    def submit(self, request) -> int:
+        """Queue a request; returns its ticket (arrival time = now on the server clock)."""
+        t = C.c_int()
+        check(lib().tecto_server_submit(self.ptr, C.byref(request), C.byref(t)), "tecto_server_submit")
+        return t.value
+
+    def tick(self, stream=None):
+        """Admit, advance every admitted world one step, retire; returns (active, waiting)."""
+        a, w = C.c_int(), C.c_int()
+        check(lib().tecto_server_tick(self.ptr, _stream(stream), C.byref(a), C.byref(w)), "tecto_server_tick")
+        return a.value, w.value
+
+    def poll(self, ticket: int):
+        """(state, RequestResult) of a ticket; state is REQUEST_WAITING / RUNNING / DONE."""
+        st, r = C.c_int(), RequestResult()
+        check(lib().tecto_server_poll(self.ptr, ticket, C.byref(st), C.byref(r)), "tecto_server_poll")
+        return st.value, r
+
+    def drain(self, stream=None, max_ticks: int = 1 << 30) -> int:
+        """Tick until nothing is admitted or waiting; returns the ticks taken."""
+        n = 0
+        while n < max_ticks:
+            a, w = self.tick(stream)
+            n += 1
+            if a == 0 and w == 0:
+                break
+        return n
+
+    def live_stats(self) -> ServerStats:
+        st = ServerStats()
+        check(lib().tecto_server_live_stats(self.ptr, C.byref(st)), "tecto_server_live_stats")
+        return st
 
     def close(self) -> None:
         if getattr(self, "ptr", None):

@@ -24,19 +24,6 @@ int batch_step_graph(Batch &b, int nsteps, cudaStream_t st, bool use_graph);
 
 using namespace tecto;
 
-struct tecto_server {
-    tecto_settings settings{};
-    size_t budget = 0;
-    int max_worlds = 0;
-    bool dry = false;
-    double dry_cost = 2e-4;  // seconds per tick per million active cells
-    tecto_batch *batch = nullptr;
-    std::string out_dir;     // where finished requests are written (tecto_server_set_output)
-    int out_what = 0;        // TECTO_SERVER_OUT_* bits
-    int init_mode = TECTO_SERVER_INIT_SYNTHETIC;
-    float out_lo = 0.0f, out_hi = 1.0f;  // height range of the 16-bit export
-};
-
 namespace {
 
 using Clock = std::chrono::steady_clock;
@@ -48,6 +35,47 @@ struct Live {
     size_t cells;
     int steps_left;
 };
+
+// Continuous-batching state, shared by a trace replay and the live API: the requests waiting for
+// admission (first come first served), the admitted worlds and the bytes they hold.
+struct Serving {
+    std::deque<int> waiting;
+    std::vector<Live> live;
+    size_t used = 0;
+    double peak = 0;
+    int ticks = 0, max_active = 0, done = 0;
+    bool changed = true;  // membership changed since the last tick
+};
+
+// Seconds since `t0`, or the simulated clock of a dry run (advanced by the cost model).
+struct ServeClock {
+    bool dry = false;
+    double v = 0;
+    Clock::time_point t0 = Clock::now();
+    double now() const { return dry ? v : std::chrono::duration<double>(Clock::now() - t0).count(); }
+};
+
+}  // namespace
+
+struct tecto_server {
+    tecto_settings settings{};
+    size_t budget = 0;
+    int max_worlds = 0;
+    bool dry = false;
+    double dry_cost = 2e-4;  // seconds per tick per million active cells
+    tecto_batch *batch = nullptr;
+    std::string out_dir;     // where finished requests are written (tecto_server_set_output)
+    int out_what = 0;        // TECTO_SERVER_OUT_* bits
+    int init_mode = TECTO_SERVER_INIT_SYNTHETIC;
+    float out_lo = 0.0f, out_hi = 1.0f;  // height range of the 16-bit export
+    // live API (tecto_server_submit / tick / poll): requests and results by ticket
+    Serving q;
+    ServeClock clock;
+    std::vector<tecto_request> reqs;
+    std::vector<tecto_request_result> results;
+};
+
+namespace {
 
 double percentile(std::vector<double> v, double q)
 {
@@ -65,7 +93,7 @@ void finish_stats(const tecto_request *req, int n, const tecto_request_result *r
     std::vector<double> lat;
     tecto_server_stats s{};
     for (int i = 0; i < n; ++i) {
-        if (res[i].status == TECTO_OK) {
+        if (res[i].status == TECTO_OK && res[i].finish_s >= 0) {
             ++s.completed;
             lat.push_back(res[i].finish_s - res[i].arrival_s);
             s.cell_updates += (double)req[i].width * (double)req[i].height * (double)req[i].steps;
@@ -133,6 +161,11 @@ int write_outputs(const tecto_server *sv, tecto_world *w, int idx, cudaStream_t 
 // request failed; serving goes on).
 void finish_world(const tecto_server *sv, tecto_world *w, int idx, cudaStream_t st, tecto_request_result &res)
 {
+    const int ok = tecto_world_check(w, (tecto_stream_t)st);  // a device-side wait that gave up fails the request
+    if (ok != TECTO_OK) {
+        res.status = ok;
+        return;
+    }
     res.height_checksum = checksum(w, st);
     if (sv->out_what) {
         const int rc = write_outputs(sv, w, idx, st);
@@ -144,6 +177,120 @@ bool valid_request(const tecto_request &r)
 {
     return r.width >= 1 && r.height >= 1 && r.plates >= 1 && r.plates <= kPlates && r.steps >= 0 &&
            (size_t)r.width * (size_t)r.height <= ((size_t)1 << 30);
+}
+
+// Drops the head of the queue if it can never be served (invalid, or larger than the whole budget);
+// returns whether it did.
+bool reject_head(const tecto_server *sv, Serving &q, const tecto_request *req, tecto_request_result *res)
+{
+    const int i = q.waiting.front();
+    const tecto_request &r = req[i];
+    int status = TECTO_OK;
+    if (!valid_request(r)) status = TECTO_ERR_INVALID;
+    else if (world_footprint(r.width, r.height) > sv->budget) status = TECTO_ERR_BUDGET;
+    if (status == TECTO_OK) return false;
+    res[i].status = status;
+    q.waiting.pop_front();
+    ++q.done;
+    return true;
+}
+
+// Admission: waiting requests join first come first served while their footprint fits the budget
+// and fewer than max_worlds are active; the first that does not fit stops admission (no overtaking).
+int admit(tecto_server *sv, Serving &q, const tecto_request *req, tecto_request_result *res, cudaStream_t st,
+          const ServeClock &c)
+{
+    while (!q.waiting.empty()) {
+        if (reject_head(sv, q, req, res)) continue;
+        const int i = q.waiting.front();
+        const tecto_request &r = req[i];
+        const size_t bytes = world_footprint(r.width, r.height);
+        if (q.used + bytes > sv->budget || (int)q.live.size() >= sv->max_worlds) break;
+        Live L{i, nullptr, bytes, (size_t)r.width * (size_t)r.height, r.steps};
+        if (!sv->dry) {
+            int rc = make_world(sv, r, st, &L.world);
+            if (rc != TECTO_OK) return rc;
+            if ((rc = tecto_batch_add(sv->batch, L.world, (tecto_stream_t)st)) != TECTO_OK) {
+                tecto_world_destroy(L.world);
+                return rc;
+            }
+        }
+        q.used += bytes;
+        q.peak = std::max(q.peak, (double)q.used);
+        res[i].admit_s = c.now();
+        q.live.push_back(L);
+        q.waiting.pop_front();
+        q.changed = true;
+    }
+    return TECTO_OK;
+}
+
+// Retires every admitted world with no steps left: its result (checksum, outputs named by `idx`),
+// then it leaves the batch and its memory returns to the budget.
+void retire(tecto_server *sv, Serving &q, tecto_request_result *res, cudaStream_t st, const ServeClock &c)
+{
+    for (size_t k = 0; k < q.live.size();) {
+        if (q.live[k].steps_left > 0) { ++k; continue; }
+        const int i = q.live[k].idx;
+        if (!sv->dry) {
+            finish_world(sv, q.live[k].world, i, st, res[i]);
+            tecto_batch_remove(sv->batch, q.live[k].world);
+            tecto_world_destroy(q.live[k].world);
+        }
+        res[i].finish_s = c.now();
+        q.used -= q.live[k].bytes;
+        q.live.erase(q.live.begin() + (long)k);
+        ++q.done;
+        q.changed = true;
+    }
+}
+
+// One tick: every admitted world advances one step as one batch, then the finished ones retire.
+int tick(tecto_server *sv, Serving &q, tecto_request_result *res, cudaStream_t st, ServeClock &c)
+{
+    q.max_active = std::max(q.max_active, (int)q.live.size());
+    if (sv->dry) {
+        size_t cells = 0;
+        for (const Live &L : q.live) cells += L.cells;
+        c.v += sv->dry_cost * (double)cells / 1e6;
+    } else {
+        // graphs pay off once the membership is stable; right after a change launch directly
+        const int rc = batch_step_graph(sv->batch->b, 1, st, !q.changed);
+        if (rc != TECTO_OK) return rc;
+        TECTO_CUDA(cudaStreamSynchronize(st));
+        if (sv->batch->b.sort.error) {  // the batch's sort look-back flag (per-world flags: at retire)
+            uint32_t e = 0;
+            TECTO_CUDA(cudaMemcpy(&e, sv->batch->b.sort.error, 4, cudaMemcpyDeviceToHost));
+            if (e) {
+                cudaMemset(sv->batch->b.sort.error, 0, 4);
+                set_error("a bounded device-side wait gave up");
+                return TECTO_ERR_DEVICE_TIMEOUT;
+            }
+        }
+    }
+    q.changed = false;
+    ++q.ticks;
+    for (Live &L : q.live) --L.steps_left;
+    retire(sv, q, res, st, c);
+    return TECTO_OK;
+}
+
+// After a failure: every admitted world leaves the batch and is freed, waiting requests are dropped.
+void drop_all(tecto_server *sv, Serving &q)
+{
+    for (Live &L : q.live) {
+        if (L.world) {
+            tecto_batch_remove(sv->batch, L.world);
+            tecto_world_destroy(L.world);
+        }
+    }
+    q = Serving{};
+}
+
+int ensure_batch(tecto_server *sv)
+{
+    if (sv->dry || sv->batch) return TECTO_OK;
+    return tecto_batch_create(&sv->batch);
 }
 
 }  // namespace
@@ -160,6 +307,7 @@ int tecto_server_create(const tecto_settings *settings, size_t budget_bytes, int
     sv->budget = budget_bytes;
     sv->max_worlds = (max_worlds <= 0 || max_worlds > kMaxBatchWorlds) ? kMaxBatchWorlds : max_worlds;
     sv->dry = (flags & TECTO_SERVER_DRY_RUN) != 0;
+    sv->clock.dry = sv->dry;
     *out = sv;
     return TECTO_OK;
 }
@@ -167,6 +315,7 @@ int tecto_server_create(const tecto_settings *settings, size_t budget_bytes, int
 int tecto_server_destroy(tecto_server *sv)
 {
     if (!sv) return TECTO_OK;
+    drop_all(sv, sv->q);
     if (sv->batch) tecto_batch_destroy(sv->batch);
     delete sv;
     return TECTO_OK;
@@ -208,11 +357,13 @@ int tecto_server_run_trace(tecto_server *sv, const tecto_request *req, int n, te
                            tecto_request_result *res, tecto_server_stats *stats)
 {
     if (!sv || (n > 0 && (!req || !res))) return TECTO_ERR_INVALID;
-    cudaStream_t st = (cudaStream_t)stream;
-    if (!sv->dry && !sv->batch) {
-        const int rc = tecto_batch_create(&sv->batch);
-        if (rc != TECTO_OK) return rc;
+    if (!sv->q.live.empty() || !sv->q.waiting.empty()) {
+        set_error("tecto_server_run_trace: live requests are pending on this server");
+        return TECTO_ERR_INVALID;
     }
+    cudaStream_t st = (cudaStream_t)stream;
+    int rc = ensure_batch(sv);
+    if (rc != TECTO_OK) return rc;
     // arrival order (stable on ties)
     std::vector<int> order(n);
     for (int i = 0; i < n; ++i) {
@@ -220,101 +371,29 @@ int tecto_server_run_trace(tecto_server *sv, const tecto_request *req, int n, te
         res[i] = tecto_request_result{TECTO_OK, req[i].arrival_s, -1.0, -1.0, 0.0f};
     }
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return req[a].arrival_s < req[b].arrival_s; });
-    std::deque<int> waiting;
-    std::vector<Live> live;
-    size_t used = 0;
-    double peak = 0, vclock = 0;  // vclock: simulated time in dry-run mode
-    int next = 0, ticks = 0, max_active = 0, done = 0;
-    const auto t0 = Clock::now();
-    auto now = [&]() {
-        return sv->dry ? vclock : std::chrono::duration<double>(Clock::now() - t0).count();
-    };
-    int rc = TECTO_OK;
-    while (done < n) {
-        double t = now();
-        while (next < n && req[order[next]].arrival_s <= t) waiting.push_back(order[next++]);
-        // admission: first come first served against the budget
-        bool changed = false;
-        while (!waiting.empty()) {
-            const int i = waiting.front();
-            const tecto_request &r = req[i];
-            if (!valid_request(r)) {
-                res[i].status = TECTO_ERR_INVALID;
-                waiting.pop_front();
-                ++done;
-                continue;
-            }
-            const size_t bytes = world_footprint(r.width, r.height);
-            if (bytes > sv->budget) {  // can never fit
-                res[i].status = TECTO_ERR_BUDGET;
-                waiting.pop_front();
-                ++done;
-                continue;
-            }
-            if (used + bytes > sv->budget || (int)live.size() >= sv->max_worlds) break;
-            Live L{i, nullptr, bytes, (size_t)r.width * (size_t)r.height, r.steps};
-            if (!sv->dry) {
-                if ((rc = make_world(sv, r, st, &L.world)) != TECTO_OK) return rc;
-                if ((rc = tecto_batch_add(sv->batch, L.world, stream)) != TECTO_OK) return rc;
-            }
-            used += bytes;
-            peak = std::max(peak, (double)used);
-            res[i].admit_s = now();
-            live.push_back(L);
-            waiting.pop_front();
-            changed = true;
-        }
-        // retire zero-step requests immediately
-        for (size_t k = 0; k < live.size();) {
-            if (live[k].steps_left > 0) { ++k; continue; }
-            const int i = live[k].idx;
-            if (!sv->dry) {
-                finish_world(sv, live[k].world, i, st, res[i]);
-                tecto_batch_remove(sv->batch, live[k].world);
-                tecto_world_destroy(live[k].world);
-            }
-            res[i].finish_s = now();
-            used -= live[k].bytes;
-            live.erase(live.begin() + (long)k);
-            ++done;
-            changed = true;
-        }
-        if (live.empty()) {
-            if (next < n && done < n) {  // idle until the next arrival
-                const double wait = req[order[next]].arrival_s - now();
-                if (sv->dry) vclock += std::max(wait, 0.0);
+    Serving q;
+    ServeClock c;
+    c.dry = sv->dry;
+    int next = 0;
+    while (q.done < n) {
+        while (next < n && req[order[next]].arrival_s <= c.now()) q.waiting.push_back(order[next++]);
+        if ((rc = admit(sv, q, req, res, st, c)) != TECTO_OK) break;
+        retire(sv, q, res, st, c);  // zero-step requests leave at once
+        if (q.live.empty()) {
+            if (next < n && q.done < n) {  // idle until the next arrival
+                const double wait = req[order[next]].arrival_s - c.now();
+                if (sv->dry) c.v += std::max(wait, 0.0);
                 else if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(wait));
             }
             continue;
         }
-        max_active = std::max(max_active, (int)live.size());
-        // one tick: every live world advances one step
-        if (sv->dry) {
-            size_t cells = 0;
-            for (const Live &L : live) cells += L.cells;
-            vclock += sv->dry_cost * (double)cells / 1e6;
-        } else {
-            // graphs pay off once the membership is stable; right after a change launch directly
-            rc = batch_step_graph(sv->batch->b, 1, st, !changed);
-            if (rc != TECTO_OK) return rc;
-            TECTO_CUDA(cudaStreamSynchronize(st));
-        }
-        ++ticks;
-        for (size_t k = 0; k < live.size();) {
-            if (--live[k].steps_left > 0) { ++k; continue; }
-            const int i = live[k].idx;
-            if (!sv->dry) {
-                finish_world(sv, live[k].world, i, st, res[i]);
-                tecto_batch_remove(sv->batch, live[k].world);
-                tecto_world_destroy(live[k].world);
-            }
-            res[i].finish_s = now();
-            used -= live[k].bytes;
-            live.erase(live.begin() + (long)k);
-            ++done;
-        }
+        if ((rc = tick(sv, q, res, st, c)) != TECTO_OK) break;
     }
-    finish_stats(req, n, res, now(), ticks, max_active, peak, stats);
+    if (rc != TECTO_OK) {
+        drop_all(sv, q);
+        return rc;
+    }
+    finish_stats(req, n, res, c.now(), q.ticks, q.max_active, q.peak, stats);
     if (!sv->dry) return tecto_batch_check(sv->batch, stream);
     return TECTO_OK;
 }
@@ -374,6 +453,72 @@ int tecto_server_run_trace_sequential(tecto_server *sv, const tecto_request *req
         res[i].finish_s = now();
     }
     finish_stats(req, n, res, now(), ticks, 1, peak, stats);
+    return TECTO_OK;
+}
+
+/* ---- live serving: requests submitted as they come, the caller drives the ticks ---------- */
+
+int tecto_server_submit(tecto_server *sv, const tecto_request *request, int *ticket)
+{
+    if (!sv || !request || !ticket || sv->reqs.size() >= ((size_t)1 << 30)) {
+        set_error("tecto_server_submit: invalid argument");
+        return TECTO_ERR_INVALID;
+    }
+    const int i = (int)sv->reqs.size();
+    const double t = sv->clock.now();
+    sv->reqs.push_back(*request);
+    sv->reqs.back().arrival_s = t;
+    sv->results.push_back(tecto_request_result{TECTO_OK, t, -1.0, -1.0, 0.0f});
+    // a request that can never be served is answered at once
+    const tecto_request &r = sv->reqs.back();
+    if (!valid_request(r)) sv->results.back().status = TECTO_ERR_INVALID;
+    else if (world_footprint(r.width, r.height) > sv->budget) sv->results.back().status = TECTO_ERR_BUDGET;
+    else sv->q.waiting.push_back(i);
+    *ticket = i;
+    return TECTO_OK;
+}
+
+int tecto_server_tick(tecto_server *sv, tecto_stream_t stream, int *active, int *waiting)
+{
+    if (!sv) return TECTO_ERR_INVALID;
+    cudaStream_t st = (cudaStream_t)stream;
+    Serving &q = sv->q;
+    int rc = ensure_batch(sv);
+    if (rc == TECTO_OK) rc = admit(sv, q, sv->reqs.data(), sv->results.data(), st, sv->clock);
+    if (rc == TECTO_OK) {
+        retire(sv, q, sv->results.data(), st, sv->clock);  // zero-step requests leave at once
+        if (!q.live.empty()) rc = tick(sv, q, sv->results.data(), st, sv->clock);
+    }
+    if (rc != TECTO_OK) {  // every request still pending fails with the error
+        for (const Live &L : q.live) sv->results[L.idx].status = rc;
+        for (int i : q.waiting) sv->results[i].status = rc;
+        drop_all(sv, q);
+    }
+    if (active) *active = (int)q.live.size();
+    if (waiting) *waiting = (int)q.waiting.size();
+    return rc;
+}
+
+int tecto_server_poll(tecto_server *sv, int ticket, int *state, tecto_request_result *result)
+{
+    if (!sv || ticket < 0 || ticket >= (int)sv->reqs.size()) {
+        set_error("tecto_server_poll: unknown ticket");
+        return TECTO_ERR_INVALID;
+    }
+    const tecto_request_result &r = sv->results[(size_t)ticket];
+    if (state)
+        *state = (r.status != TECTO_OK || r.finish_s >= 0) ? TECTO_REQUEST_DONE
+                 : r.admit_s >= 0                         ? TECTO_REQUEST_RUNNING
+                                                          : TECTO_REQUEST_WAITING;
+    if (result) *result = r;
+    return TECTO_OK;
+}
+
+int tecto_server_live_stats(tecto_server *sv, tecto_server_stats *stats)
+{
+    if (!sv || !stats) return TECTO_ERR_INVALID;
+    finish_stats(sv->reqs.data(), (int)sv->reqs.size(), sv->results.data(), sv->clock.now(), sv->q.ticks,
+                 sv->q.max_active, sv->q.peak, stats);
     return TECTO_OK;
 }
 
