@@ -621,6 +621,8 @@ def run_case(args):
     erosion2048  one 5-iteration thermal launch and one fused hydraulic launch on a 2048^2 world;
     plain2048    4 steps of one 2048^2 world, 32 plates;
     policy2048   the same with plate dynamics, relabel after a CCL on every step, and merges;
+    collide2048  three collide phases (advection fused into the sort, winner pick, collision types)
+                 of one 2048^2 world, 32 plates, 8-bit sort digits;
     batch        the mixed-size batch with the default tile and digit width, 4 steps."""
     import torch
 
@@ -644,6 +646,13 @@ def run_case(args):
         w = T.World(s, 2048, 2048, seed=1000)
         w.init_synthetic_device(32, 1.0, 1)
         w.step(4, stream)
+        w.check(stream)
+    elif args.case == "collide2048":
+        s.step.sortRadixBits = 8
+        w = T.World(s, 2048, 2048, seed=1000)
+        w.init_synthetic_device(32, 1.0, 1)
+        for _ in range(3):
+            w.collide(stream)
         w.check(stream)
     elif args.case == "plain2048":
         w = T.World(s, 2048, 2048, seed=1000)
@@ -674,7 +683,7 @@ def main():
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
     ap.add_argument("--serve-requests", type=int, default=64)
     ap.add_argument("--quick", action="store_true", help="headline only (no plain/served/large-world lines)")
-    ap.add_argument("--case", choices=["erosion2048", "plain2048", "policy2048", "batch"],
+    ap.add_argument("--case", choices=["erosion2048", "plain2048", "policy2048", "collide2048", "batch"],
                     help="a small fixed workload for profilers")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
