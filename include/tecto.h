@@ -503,7 +503,9 @@ int tecto_server_set_dry_cost(tecto_server *server, double seconds_per_mcell_ste
  * against the budget, advances every admitted world one step as one batch, and retires the worlds
  * that are done (checksum, and the outputs of tecto_server_set_output named request_<ticket>);
  * with nothing admitted it does no device work.  It reports the admitted and waiting counts after
- * the tick.  If a tick fails, every pending request takes its error as status and leaves.
+ * the tick.  A request whose world cannot be created (out of device memory, say) is done with that
+ * error as its status, in a trace replay too; if a tick fails, every pending request takes its
+ * error as status and leaves.
  * tecto_server_poll gives a ticket's state and result; tecto_server_live_stats summarises the
  * submitted requests (wall_s = the server clock now).  One host thread owns a server;
  * tecto_server_run_trace is refused while live requests are pending. */

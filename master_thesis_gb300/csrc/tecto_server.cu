@@ -197,7 +197,7 @@ bool reject_head(const tecto_server *sv, Serving &q, const tecto_request *req, t
 
 // Admission: waiting requests join first come first served while their footprint fits the budget
 // and fewer than max_worlds are active; the first that does not fit stops admission (no overtaking).
-int admit(tecto_server *sv, Serving &q, const tecto_request *req, tecto_request_result *res, cudaStream_t st,
+void admit(tecto_server *sv, Serving &q, const tecto_request *req, tecto_request_result *res, cudaStream_t st,
           const ServeClock &c)
 {
     while (!q.waiting.empty()) {
@@ -208,11 +208,15 @@ int admit(tecto_server *sv, Serving &q, const tecto_request *req, tecto_request_
         if (q.used + bytes > sv->budget || (int)q.live.size() >= sv->max_worlds) break;
         Live L{i, nullptr, bytes, (size_t)r.width * (size_t)r.height, r.steps};
         if (!sv->dry) {
+            // a world that cannot be created (out of memory, say) fails its own request only
             int rc = make_world(sv, r, st, &L.world);
-            if (rc != TECTO_OK) return rc;
-            if ((rc = tecto_batch_add(sv->batch, L.world, (tecto_stream_t)st)) != TECTO_OK) {
+            if (rc == TECTO_OK && (rc = tecto_batch_add(sv->batch, L.world, (tecto_stream_t)st)) != TECTO_OK)
                 tecto_world_destroy(L.world);
-                return rc;
+            if (rc != TECTO_OK) {
+                res[i].status = rc;
+                q.waiting.pop_front();
+                ++q.done;
+                continue;
             }
         }
         q.used += bytes;
@@ -222,7 +226,6 @@ int admit(tecto_server *sv, Serving &q, const tecto_request *req, tecto_request_
         q.waiting.pop_front();
         q.changed = true;
     }
-    return TECTO_OK;
 }
 
 // Retires every admitted world with no steps left: its result (checksum, outputs named by `idx`),
@@ -377,7 +380,7 @@ int tecto_server_run_trace(tecto_server *sv, const tecto_request *req, int n, te
     int next = 0;
     while (q.done < n) {
         while (next < n && req[order[next]].arrival_s <= c.now()) q.waiting.push_back(order[next++]);
-        if ((rc = admit(sv, q, req, res, st, c)) != TECTO_OK) break;
+        admit(sv, q, req, res, st, c);
         retire(sv, q, res, st, c);  // zero-step requests leave at once
         if (q.live.empty()) {
             if (next < n && q.done < n) {  // idle until the next arrival
@@ -484,7 +487,7 @@ int tecto_server_tick(tecto_server *sv, tecto_stream_t stream, int *active, int 
     cudaStream_t st = (cudaStream_t)stream;
     Serving &q = sv->q;
     int rc = ensure_batch(sv);
-    if (rc == TECTO_OK) rc = admit(sv, q, sv->reqs.data(), sv->results.data(), st, sv->clock);
+    if (rc == TECTO_OK) admit(sv, q, sv->reqs.data(), sv->results.data(), st, sv->clock);
     if (rc == TECTO_OK) {
         retire(sv, q, sv->results.data(), st, sv->clock);  // zero-step requests leave at once
         if (!q.live.empty()) rc = tick(sv, q, sv->results.data(), st, sv->clock);
