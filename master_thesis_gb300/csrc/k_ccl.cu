@@ -103,9 +103,21 @@ __device__ __forceinline__ const WorldDev *ccl_tile(const WorldDev *worlds, cons
     return wd;
 }
 
+// One warp per tile row (CX is the warp width).  A row's left edges make runs: every cell's
+// parent starts as the first cell of its run, found with one ballot, without atomics.  Up edges
+// then join runs; an up edge is skipped when an edge already kept joins the same two runs:
+//   t(x)  when x is joined to x - 1 and x - 1 has t or tr (same target, or the target's left
+//         neighbour, joined to it by the left edge all modes include);
+//   tl(x) when x is joined to x - 1 and x - 1 has t or tl;
+//   tr(x) when x has t, or x is joined to x - 1 and x - 1 has tr.
+// A skip depends only on edges strictly earlier in (column, t before tr) order, so every skipped
+// edge's runs are already joined by kept ones: the components, and their minimum-index roots, are
+// those of the full edge set.  Edges whose neighbour lies in the tile only through the torus wrap
+// (a tile spanning the whole world) take the plain union.
 __global__ __launch_bounds__(256) void k_ccl_local(const WorldDev *worlds, const uint2 *tiles, int cur_id,
                                                    int mode, int period)
 {
+    static_assert(CX == 32, "one warp per tile row");
     __shared__ int par[CX * CY];
     int x0, y0;
     const WorldDev *wd = ccl_tile(worlds, tiles, period, &x0, &y0);
@@ -114,29 +126,71 @@ __global__ __launch_bounds__(256) void k_ccl_local(const WorldDev *worlds, const
     uint32_t *labels = wd->labels;
     const int W = wd->W, H = wd->H;
     const int tw = min(CX, W - x0), th = min(CY, H - y0);
-    for (int e = threadIdx.x; e < CX * CY; e += blockDim.x) par[e] = e;
-    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr int kRowsPerWarp = CY / 8;
     const int dxs[4] = {-1, 0, -1, 1}, dys[4] = {0, -1, -1, -1};
-    for (int e = threadIdx.x; e < CX * CY; e += blockDim.x) {
-        const int ly = e / CX, lx = e - ly * CX;
-        if (lx >= tw || ly >= th) continue;
-        const int x = x0 + lx, y = y0 + ly;
-        const unsigned m = edge_mask(id, x, y, W, H, mode);
+    unsigned keep[kRowsPerWarp], wrapped[kRowsPerWarp];
+#pragma unroll
+    for (int r = 0; r < kRowsPerWarp; ++r) {
+        const int ly = warp + 8 * r;
+        const int x = x0 + lane, y = y0 + ly;
+        const bool valid = lane < tw && ly < th;
+        unsigned m = valid ? edge_mask(id, x, y, W, H, mode) : 0u;
+        // natural: the neighbour is the adjacent cell of the tile, no wrap; wrapped: inside the
+        // tile only through the wrap; edges leaving the tile belong to k_ccl_border
+        unsigned nat = 0, wrp = 0;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             if (!(m & (1u << k))) continue;
-            const int nx = wrapc(x + dxs[k], W), ny = wrapc(y + dys[k], H);
-            const int nlx = nx - x0, nly = ny - y0;
-            if (nlx >= 0 && nlx < tw && nly >= 0 && nly < th) smem_union(par, e, nly * CX + nlx);
+            const int ax = lane + dxs[k], ay = ly + dys[k];
+            if (ax >= 0 && ax < tw && ay >= 0) {
+                nat |= 1u << k;
+            } else {
+                const int nlx = wrapc(x + dxs[k], W) - x0, nly = wrapc(y + dys[k], H) - y0;
+                if (nlx >= 0 && nlx < tw && nly >= 0 && nly < th) wrp |= 1u << k;
+            }
+        }
+        // runs of the row: a cell without a natural left edge starts one
+        const unsigned starts = __ballot_sync(0xffffffffu, !(nat & 1u));
+        par[ly * CX + lane] = ly * CX + (31 - __clz(starts & (0xffffffffu >> (31 - lane))));
+        const unsigned prev = __shfl_up_sync(0xffffffffu, nat, 1);
+        unsigned up = nat & 14u;
+        if (nat & 1u) {  // joined to x - 1 (lane > 0)
+            if (prev & (2u | 8u)) up &= ~2u;
+            if (prev & (2u | 4u)) up &= ~4u;
+            if (prev & 8u) up &= ~8u;
+        }
+        if (nat & 2u) up &= ~8u;
+        keep[r] = up;
+        wrapped[r] = wrp;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kRowsPerWarp; ++r) {
+        const int ly = warp + 8 * r;
+        const int e = ly * CX + lane;
+        const unsigned up = keep[r], wrp = wrapped[r];
+        if (up & 2u) smem_union(par, e, e - CX);
+        if (up & 4u) smem_union(par, e, e - CX - 1);
+        if (up & 8u) smem_union(par, e, e - CX + 1);
+        if (wrp) {
+            const int x = x0 + lane, y = y0 + ly;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if (!(wrp & (1u << k))) continue;
+                const int nlx = wrapc(x + dxs[k], W) - x0, nly = wrapc(y + dys[k], H) - y0;
+                smem_union(par, e, nly * CX + nlx);
+            }
         }
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < CX * CY; e += blockDim.x) {
-        const int ly = e / CX, lx = e - ly * CX;
-        if (lx >= tw || ly >= th) continue;
-        const int r = smem_find(par, e);
-        const int ry = r / CX, rx = r - ry * CX;
-        labels[(size_t)(y0 + ly) * W + x0 + lx] = (uint32_t)((y0 + ry) * W + x0 + rx);
+#pragma unroll
+    for (int r = 0; r < kRowsPerWarp; ++r) {
+        const int ly = warp + 8 * r;
+        if (lane >= tw || ly >= th) continue;
+        const int root = smem_find(par, ly * CX + lane);
+        const int ry = root / CX, rx = root - ry * CX;
+        labels[(size_t)(y0 + ly) * W + x0 + lane] = (uint32_t)((y0 + ry) * W + x0 + rx);
     }
 }
 

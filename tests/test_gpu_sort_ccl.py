@@ -89,6 +89,15 @@ def id_maps():
     yield "diag_50x90", diag
     _, ids, _ = T.generate_world(300, 170, 12, 1.0, 9)
     yield "voronoi_300x170", ids
+    # one tile spans the whole world: edges wrap back into the same tile
+    yield "random2_32x16", rng.integers(0, 2, (16, 32)).astype(np.uint8)
+    yield "random2_32x5", rng.integers(0, 2, (5, 32)).astype(np.uint8)
+    yield "checker_48x20", np.fromfunction(lambda y, x: (x + y) % 2, (20, 48)).astype(np.uint8)
+    yield "random4_33x17", rng.integers(0, 4, (17, 33)).astype(np.uint8)
+    # long horizontal runs broken by sparse dots: run starts and skipped up edges
+    runs = np.zeros((40, 100), np.uint8)
+    runs[rng.integers(0, 40, 120), rng.integers(0, 100, 120)] = 1
+    yield "sparse_dots_100x40", runs
 
 
 @pytest.mark.parametrize("mode", [T.CCL_4, T.CCL_8, T.CCL_REF8])
