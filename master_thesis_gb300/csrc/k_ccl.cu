@@ -10,7 +10,7 @@
 //                  (ccl.cu:107-116), plus top and top-right on row 0 (ccl.cu:161-170).
 // (Edges are undirected; each is generated once, from the lower-right cell.)
 //
-// Three kernels: union-find inside a 32x16 tile in shared memory (roots = smallest index),
+// Three kernels: union-find inside a 32x32 tile in shared memory (roots = smallest index),
 // unions across tile borders with global atomicMin linking, and a flatten pass.
 #include "tecto_internal.cuh"
 
@@ -18,7 +18,7 @@ namespace tecto {
 
 namespace {
 
-constexpr int CX = 32, CY = 16;
+constexpr int CX = kCclTileX, CY = kCclTileY;
 
 // Edge mask of cell (x, y): bit 0 l, bit 1 t, bit 2 tl, bit 3 tr.
 __device__ __forceinline__ unsigned edge_mask(const uint8_t *id, int x, int y, int W, int H, int mode)
@@ -117,7 +117,7 @@ __device__ __forceinline__ const WorldDev *ccl_tile(const WorldDev *worlds, cons
 __global__ __launch_bounds__(256) void k_ccl_local(const WorldDev *worlds, const uint2 *tiles, int cur_id,
                                                    int mode, int period)
 {
-    static_assert(CX == 32, "one warp per tile row");
+    static_assert(CX == 32 && CY % 8 == 0, "one warp per tile row, eight warps");
     __shared__ int par[CX * CY];
     int x0, y0;
     const WorldDev *wd = ccl_tile(worlds, tiles, period, &x0, &y0);

@@ -159,6 +159,8 @@ struct UpliftRefScratch {
 
 // Phase work lists.
 enum TileKind { TK_RESOLVE = 0, TK_THERMAL, TK_HYDRO, TK_CCL, TK_STATS, TK_COUNT };
+// CCL tiles: one warp per row of kCclTileX cells, kCclTileY rows per block
+constexpr int kCclTileX = 32, kCclTileY = 32;
 
 // One batch: members, their device table, work lists and the batch-level buffers.
 struct Batch {
