@@ -9,8 +9,10 @@
 // then each pass is one kernel that ranks a tile of 4096 keys with warp ballots, publishes the
 // tile's digit counts, walks back over earlier tiles (decoupled look-back, bounded spin) and
 // scatters through shared memory so that runs of equal digits leave as contiguous stores.
-// The first pass can generate its keys from plate ids (advection fused into the sort: the key
-// of cell i is getPixelMovements' wrapped destination, plate_tectonics_kernel.cu:248-265).
+// The keys can be generated from plate ids (advection fused into the sort: the key of cell i is
+// getPixelMovements' wrapped destination, plate_tectonics_kernel.cu:248-265): the histogram
+// kernel generates them once, counts them and stores them for the first pass, whose values are
+// then the cell indices themselves.
 //
 // The digit width RB is a template parameter (8..11 bits): wider digits mean fewer passes over
 // the keys but larger per-tile histograms and look-back tables; the autotuner picks per size.
@@ -33,12 +35,12 @@ struct Digits {
 };
 
 // Dynamic shared memory of one pass: per-warp digit counts, per-digit tile start and global
-// base, the staged keys and values, and (key generation) the batch's world bases.
+// base, the staged keys and values.
 template <int RB>
-constexpr size_t pass_smem(bool gen)
+constexpr size_t pass_smem()
 {
-    return ((size_t)kWarps * Digits<RB>::R + 2 * (size_t)Digits<RB>::R + 2 * (size_t)kSortTile +
-            (gen ? (size_t)kMaxBatchWorlds + 1 : 0)) * sizeof(uint32_t);
+    return ((size_t)kWarps * Digits<RB>::R + 2 * (size_t)Digits<RB>::R + 2 * (size_t)kSortTile) *
+           sizeof(uint32_t);
 }
 
 // Batch-virtual destination of virtual cell i: the owning world's getPixelMovements destination
@@ -77,10 +79,10 @@ __device__ __forceinline__ void st_volatile(uint32_t *p, uint32_t v)
     *(volatile uint32_t *)p = v;
 }
 
-// Digit histograms of all passes in one read of the keys.
+// Digit histograms of all passes in one read of the keys; generated keys are stored to keys_gen.
 template <bool GEN, int RB>
 __global__ __launch_bounds__(256) void k_sort_hist(GenArgs g, const uint32_t *keys_in, size_t n,
-                                                   int passes, uint32_t *hist)
+                                                   int passes, uint32_t *hist, uint32_t *keys_gen)
 {
     using D = Digits<RB>;
     __shared__ uint32_t s_hist[D::MAX_PASSES][D::R];
@@ -96,7 +98,14 @@ __global__ __launch_bounds__(256) void k_sort_hist(GenArgs g, const uint32_t *ke
         const size_t i = r * stride + (size_t)blockIdx.x * blockDim.x + threadIdx.x;
         const bool valid = i < n;
         uint32_t key = 0;
-        if (valid) key = GEN ? gen_key(i, g, s_vbase) : keys_in[i];
+        if (valid) {
+            if (GEN) {
+                key = gen_key(i, g, s_vbase);
+                keys_gen[i] = key;
+            } else {
+                key = keys_in[i];
+            }
+        }
         for (int p = 0; p < passes; ++p) {
             const uint32_t d = valid ? ((key >> (RB * p)) & D::MASK) : (uint32_t)D::R;
             const unsigned peers = __match_any_sync(0xffffffffu, d);
@@ -156,12 +165,11 @@ __global__ void k_sort_scan(uint32_t *hist, int passes)
     }
 }
 
-// One onesweep pass.
-template <bool GEN, int RB>
+// One onesweep pass.  vals_in == nullptr: the value of position i is i.
+template <int RB>
 __global__ __launch_bounds__(kSortThreads) void k_sort_pass(
-    GenArgs g, const uint32_t *keys_in,
-    const uint32_t *vals_in, uint32_t *keys_out, uint32_t *vals_out, size_t n, int shift,
-    const uint32_t *digit_start, uint32_t *status, uint32_t *tile_counter, uint32_t *error)
+    const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_out, uint32_t *vals_out, size_t n,
+    int shift, const uint32_t *digit_start, uint32_t *status, uint32_t *tile_counter, uint32_t *error)
 {
     using D = Digits<RB>;
     constexpr int R = D::R, DPT = D::DPT;
@@ -171,14 +179,12 @@ __global__ __launch_bounds__(kSortThreads) void k_sort_pass(
     uint32_t *s_base = s_start + R;              // global output position of the digit's run
     uint32_t *s_keys = s_base + R;
     uint32_t *s_vals = s_keys + kSortTile;
-    uint32_t *s_vbase = s_vals + kSortTile;      // key generation only
     __shared__ uint32_t s_w[kWarps];
     __shared__ uint32_t s_tile;
 
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     if (t == 0) s_tile = atomicAdd(tile_counter, 1u);
     for (int i = t; i < kWarps * R; i += kSortThreads) s_cnt[i] = 0;
-    if (GEN) load_vbase(g, s_vbase);
     __syncthreads();
     const uint32_t tile = s_tile;
     const size_t base = (size_t)tile * kSortTile;
@@ -189,13 +195,8 @@ __global__ __launch_bounds__(kSortThreads) void k_sort_pass(
     for (int it = 0; it < kSortItems; ++it) {
         const size_t idx = wbase + (size_t)it * 32 + lane;
         if (idx < n) {
-            if (GEN) {
-                k[it] = gen_key(idx, g, s_vbase);
-                v[it] = (uint32_t)idx;
-            } else {
-                k[it] = keys_in[idx];
-                v[it] = vals_in[idx];
-            }
+            k[it] = keys_in[idx];
+            v[it] = vals_in ? vals_in[idx] : (uint32_t)idx;
         } else {
             k[it] = 0;
             v[it] = 0;
@@ -334,10 +335,8 @@ size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 template <int RB>
 int set_sort_attributes()
 {
-    TECTO_CUDA(cudaFuncSetAttribute(k_sort_pass<true, RB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)pass_smem<RB>(true)));
-    TECTO_CUDA(cudaFuncSetAttribute(k_sort_pass<false, RB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)pass_smem<RB>(false)));
+    TECTO_CUDA(cudaFuncSetAttribute(k_sort_pass<RB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)pass_smem<RB>()));
     return TECTO_OK;
 }
 
@@ -357,23 +356,22 @@ int run_sort_rb(const SortArgs &a, const SortScratch &scr, cudaStream_t st, int 
     const GenArgs g{a.worlds, a.vbase, a.nworlds, a.cur_id};
     int hist_blocks = (int)((a.n + 255) / 256);
     if (hist_blocks > 152 * 8) hist_blocks = 152 * 8;
-    if (gen)
-        k_sort_hist<true, RB><<<hist_blocks, 256, 0, st>>>(g, nullptr, a.n, passes, scr.hist);
-    else
-        k_sort_hist<false, RB><<<hist_blocks, 256, 0, st>>>(g, a.keys_in, a.n, passes, scr.hist);
+    // generated keys go to the second key half, which the first pass reads and does not write
+    const uint32_t *kin = a.keys_in, *vin = a.vals_in;
+    if (gen) {
+        k_sort_hist<true, RB><<<hist_blocks, 256, 0, st>>>(g, nullptr, a.n, passes, scr.hist, a.keys[1]);
+        kin = a.keys[1];
+        vin = nullptr;
+    } else {
+        k_sort_hist<false, RB><<<hist_blocks, 256, 0, st>>>(g, a.keys_in, a.n, passes, scr.hist, nullptr);
+    }
     k_sort_scan<RB><<<1, kSortThreads, 0, st>>>(scr.hist, passes);
     int half = 0;
-    const uint32_t *kin = a.keys_in, *vin = a.vals_in;
     for (int p = 0; p < passes; ++p) {
         uint32_t *kout = a.keys[half], *vout = a.vals[half];
         uint32_t *status = scr.status + (size_t)p * tiles * R;
-        if (p == 0 && gen)
-            k_sort_pass<true, RB><<<(unsigned)tiles, kSortThreads, pass_smem<RB>(true), st>>>(
-                g, nullptr, nullptr, kout, vout, a.n, 0, scr.hist, status, scr.counters + p, scr.error);
-        else
-            k_sort_pass<false, RB><<<(unsigned)tiles, kSortThreads, pass_smem<RB>(false), st>>>(
-                g, kin, vin, kout, vout, a.n, RB * p, scr.hist + (size_t)p * R, status, scr.counters + p,
-                scr.error);
+        k_sort_pass<RB><<<(unsigned)tiles, kSortThreads, pass_smem<RB>(), st>>>(
+            kin, vin, kout, vout, a.n, RB * p, scr.hist + (size_t)p * R, status, scr.counters + p, scr.error);
         kin = kout;
         vin = vout;
         half ^= 1;
