@@ -20,14 +20,12 @@ namespace {
 
 constexpr int CX = kCclTileX, CY = kCclTileY;
 
-// Edge mask of cell (x, y): bit 0 l, bit 1 t, bit 2 tl, bit 3 tr.
-__device__ __forceinline__ unsigned edge_mask(const uint8_t *id, int x, int y, int W, int H, int mode)
+// Edge mask of a cell on row y from its id c and its neighbours' ids: bit 0 l, bit 1 t, bit 2 tl,
+// bit 3 tr.
+__device__ __forceinline__ unsigned mask_of(unsigned c, unsigned l, unsigned t, unsigned tl, unsigned tr, int y,
+                                            int mode)
 {
-    const uint8_t c = id[(size_t)y * W + x];
-    const bool el = id[cidx(x - 1, y, W, H)] == c;
-    const bool et = id[cidx(x, y - 1, W, H)] == c;
-    const bool etl = id[cidx(x - 1, y - 1, W, H)] == c;
-    const bool etr = id[cidx(x + 1, y - 1, W, H)] == c;
+    const bool el = l == c, et = t == c, etl = tl == c, etr = tr == c;
     if (mode == TECTO_CCL_4) return (el ? 1u : 0u) | (et ? 2u : 0u);
     if (mode == TECTO_CCL_8) return (el ? 1u : 0u) | (et ? 2u : 0u) | (etl ? 4u : 0u) | (etr ? 8u : 0u);
     unsigned m = (el ? 1u : 0u) | (etl ? 4u : 0u);
@@ -38,6 +36,12 @@ __device__ __forceinline__ unsigned edge_mask(const uint8_t *id, int x, int y, i
         else if (etr) m |= 8u;
     }
     return m;
+}
+
+__device__ __forceinline__ unsigned edge_mask(const uint8_t *id, int x, int y, int W, int H, int mode)
+{
+    return mask_of(id[(size_t)y * W + x], id[cidx(x - 1, y, W, H)], id[cidx(x, y - 1, W, H)],
+                   id[cidx(x - 1, y - 1, W, H)], id[cidx(x + 1, y - 1, W, H)], y, mode);
 }
 
 __device__ __forceinline__ int smem_find(const int *par, int a)
@@ -135,7 +139,20 @@ __global__ __launch_bounds__(256) void k_ccl_local(const WorldDev *worlds, const
         const int ly = warp + 8 * r;
         const int x = x0 + lane, y = y0 + ly;
         const bool valid = lane < tw && ly < th;
-        unsigned m = valid ? edge_mask(id, x, y, W, H, mode) : 0u;
+        // the row and the row above, one byte per lane; the left and right neighbours come from
+        // the adjacent lanes, the row ends load theirs (wrapped)
+        const int yu = y == 0 ? H - 1 : y - 1;
+        const unsigned c = valid ? id[(size_t)y * W + x] : 0u;
+        const unsigned t = valid ? id[(size_t)yu * W + x] : 0u;
+        unsigned l = __shfl_up_sync(0xffffffffu, c, 1), tl = __shfl_up_sync(0xffffffffu, t, 1);
+        unsigned tr = __shfl_down_sync(0xffffffffu, t, 1);
+        if (valid && lane == 0) {
+            const int xl = x == 0 ? W - 1 : x - 1;
+            l = id[(size_t)y * W + xl];
+            tl = id[(size_t)yu * W + xl];
+        }
+        if (valid && lane == tw - 1) tr = id[(size_t)yu * W + (x + 1 == W ? 0 : x + 1)];
+        unsigned m = valid ? mask_of(c, l, t, tl, tr, y, mode) : 0u;
         // natural: the neighbour is the adjacent cell of the tile, no wrap; wrapped: inside the
         // tile only through the wrap; edges leaving the tile belong to k_ccl_border
         unsigned nat = 0, wrp = 0;
