@@ -154,6 +154,31 @@ def test_server_writes_finished_requests(tmp_path, stream):
         np.testing.assert_array_equal(px, T.plate_palette()[w.download(T.FIELD_PLATE_ID, stream)])
 
 
+def test_live_server_writes_finished_tickets(tmp_path, stream):
+    """Live serving writes each finished ticket's files, named by ticket, byte-identical to the
+    files a trace replay writes for the same requests."""
+    s = T.baseline_settings()
+    reqs = [T.Request(width=W, height=H, plates=p, steps=st, velRange=1.0, genSeed=500 + i, worldSeed=700 + i,
+                      arrival_s=0.0)
+            for i, (W, H, p, st) in enumerate([(64, 32, 5, 2), (40, 40, 4, 3), (96, 64, 7, 0)])]
+    what = T.SERVER_OUT_HEIGHT_PNG | T.SERVER_OUT_SNAPSHOT
+    live, trace = tmp_path / "live", tmp_path / "trace"
+    live.mkdir()
+    trace.mkdir()
+    sv = T.Server(s, 2 * T.world_bytes(96, 64), max_worlds=2)
+    sv.set_output(live, what, -500.0, 500.0)
+    tickets = [sv.submit(q) for q in reqs]
+    sv.drain(stream)
+    assert all(sv.poll(t)[0] == T.REQUEST_DONE and sv.poll(t)[1].status == 0 for t in tickets)
+    sv.set_output(trace, what, -500.0, 500.0)
+    res, st = sv.run_trace(reqs, stream)
+    assert st.completed == len(reqs)
+    sv.close()
+    for t in tickets:
+        for suffix in ("_height.png", ".snap"):
+            assert (live / f"request_{t}{suffix}").read_bytes() == (trace / f"request_{t}{suffix}").read_bytes()
+
+
 def test_server_output_to_a_missing_directory_fails_the_request(tmp_path, stream):
     sv = T.Server(T.baseline_settings(), T.world_bytes(64, 64) * 2, max_worlds=2)
     sv.set_output(tmp_path / "missing", T.SERVER_OUT_SNAPSHOT)
