@@ -19,6 +19,7 @@ and sort digit width picked by the autotuner.  Beside it:
                cell-updates/s, and a saturated trace (all requests at t=0) for capacity;
   plain_2048   one 2048^2 world, 32 plates (plain path; its k_hydro roofline);
   plain_8192   one 8192^2 world, 64 plates, velocities in [-2, 2], 8-connected CCL every step.
+`issue_roofline` sets the same k_hydro launches against the SMs' instruction-issue limit, its actual bound.
 `e2e` repeats the headline through the C ABI with host buffers (packed: one buffer per field for all
 worlds; copies on a second stream overlap the previous or next step's compute): every step uploads each world's
 state from pinned host memory, steps the batch, downloads heights and plate ids, and waits for them.
@@ -72,6 +73,29 @@ def profiled_traffic_per_cell():
         return None
     m = re.search(r"traffic_bytes_per_launch_2048:\s*([0-9.eE+]+)", p.read_text())
     return float(m.group(1)) / (2048 * 2048) if m else None
+
+
+def profiled_instructions_per_cell():
+    """Warp-instructions per cell of one k_hydro launch, from the committed ncu summary (2048^2)."""
+    p = ROOT / "profiles" / "k_hydro_2048.md"
+    if not p.exists():
+        return None
+    m = re.search(r"warp_instructions_per_launch_2048:\s*([0-9.eE+]+)", p.read_text())
+    return float(m.group(1)) / (2048 * 2048) if m else None
+
+
+def issue_roofline(ipc, cells, ms, sm_mhz, sms):
+    """k_hydro against the issue limit: every SM issues at most one warp-instruction per cycle on
+    each of its four schedulers."""
+    if ipc is None or not sm_mhz or not sms:
+        return None
+    achieved = ipc * cells / (ms / 1e3) / 1e9
+    peak = sms * 4 * sm_mhz * 1e6 / 1e9
+    return {"bound": "issue", "kernel": "k_hydro", "achieved": achieved, "peak": peak,
+            "unit": "G warp-instructions/s", "frac": achieved / peak,
+            "note": "warp-instructions per cell from one ncu capture of a 2048^2 launch (edge tiles of "
+                    "small worlds issue more, so the batch figure is a lower bound); peak = SMs x 4 "
+                    "schedulers x the SM clock sampled during the timed region"}
 
 
 class ClockSampler:
@@ -370,6 +394,8 @@ def run_engine(args, ws, rank, local):
     peak, peak_src = measured_peak_hbm()
     achieved = HYDRO_BYTES_PER_CELL * total / (hydro_ms / 1e3) / 1e9
     tpc = profiled_traffic_per_cell()
+    ipc = profiled_instructions_per_cell()
+    n_sms = torch.cuda.get_device_properties(local).multi_processor_count
 
     # e2e through the C ABI with host buffers: upload every world's state, step, download
     # heights and plate ids
@@ -454,6 +480,7 @@ def run_engine(args, ws, rank, local):
                          "traffic_note": "ncu dram bytes of a 2048^2 launch, scaled per cell",
                          "peak_source": peak_src, "ms_per_launch": hydro_ms,
                          "alg_bytes_per_launch": HYDRO_BYTES_PER_CELL * total},
+            "issue_roofline": issue_roofline(ipc, total, hydro_ms, clk.summary().get("sm_mhz"), n_sms),
             "step_roofline": {"alg_bytes_per_cell": STEP_BYTES_PER_CELL,
                               "achieved_gbs": STEP_BYTES_PER_CELL * value / ws / 1e9,
                               "frac": STEP_BYTES_PER_CELL * value / ws / 1e9 / peak},
