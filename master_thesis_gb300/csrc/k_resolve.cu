@@ -195,8 +195,10 @@ __device__ __forceinline__ float resolve_cell(const ResolveParams &p, const Reso
     return writeH;
 }
 
+// Six blocks per SM (40 registers): the kernel waits mostly on its gathers from the arrival
+// sources, and the extra resident warps hide them.
 template <int R, bool DYN>
-__global__ __launch_bounds__(256) void k_resolve(ResolveParams p)
+__global__ __launch_bounds__(256, 6) void k_resolve(ResolveParams p)
 {
     constexpr int SX = RX + 2 * R, SY = RY + 2 * R;
     __shared__ uint32_t s_word[SY * SX];
