@@ -65,3 +65,20 @@ def test_job_rate_aggregates_ranks():
 
     assert bench.job_rate(1, 1000, 4, 2.0) == pytest.approx(2.0e6)
     assert bench.job_rate(4, 1000, 4, 2.0) == pytest.approx(8.0e6)
+
+
+def test_rooflines_from_the_committed_profiles():
+    """The per-cell DRAM traffic and warp-instruction counts bench.py reports come from the committed
+    ncu summary of a 2048^2 k_hydro launch; the issue roofline is achieved / (SMs x 4 x clock)."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    tpc, ipc = bench.profiled_traffic_per_cell(), bench.profiled_instructions_per_cell()
+    assert tpc is not None and 40 < tpc < 80          # about 50 B/cell against 56 algorithmic
+    assert ipc is not None and 5 < ipc < 40           # warp-instructions per cell
+    r = bench.issue_roofline(ipc, 2048 * 2048, 0.1, 2070.0, 152)
+    assert r["bound"] == "issue" and abs(r["peak"] - 152 * 4 * 2.07) < 1e-9
+    assert abs(r["achieved"] - ipc * 2048 * 2048 / 1e-4 / 1e9) < 1e-6
+    assert 0 < r["frac"] < 1
+    assert bench.issue_roofline(None, 1, 1.0, 2070.0, 152) is None
+    assert bench.issue_roofline(ipc, 1, 1.0, None, 152) is None
