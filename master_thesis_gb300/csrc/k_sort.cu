@@ -24,6 +24,9 @@ namespace {
 
 constexpr int kWarps = kSortThreads / 32;
 constexpr int kLookAhead = 8;  // predecessor tiles read per look-back round
+// From this many tiles (16 M keys) a pass runs three blocks per SM: measured faster at 67 M keys
+// (8192^2) and slower at 4 M (2048^2)
+constexpr size_t kSortWideTiles = 4096;
 
 template <int RB>
 struct Digits {
@@ -165,9 +168,12 @@ __global__ void k_sort_scan(uint32_t *hist, int passes)
     }
 }
 
-// One onesweep pass.  vals_in == nullptr: the value of position i is i.
+// One onesweep pass.  vals_in == nullptr: the value of position i is i.  Two kernels share the
+// body: k_sort_pass (the compiler takes 128 registers, two blocks per SM, no spill) for small sorts,
+// and k_sort_pass_wide (three blocks per SM, 80 registers, a few bytes of spill) once there are
+// enough tiles to fill the extra residency.
 template <int RB>
-__global__ __launch_bounds__(kSortThreads) void k_sort_pass(
+__device__ __forceinline__ void sort_pass_body(
     const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_out, uint32_t *vals_out, size_t n,
     int shift, const uint32_t *digit_start, uint32_t *status, uint32_t *tile_counter, uint32_t *error)
 {
@@ -330,12 +336,30 @@ __global__ __launch_bounds__(kSortThreads) void k_sort_pass(
     }
 }
 
+template <int RB>
+__global__ __launch_bounds__(kSortThreads) void k_sort_pass(
+    const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_out, uint32_t *vals_out, size_t n,
+    int shift, const uint32_t *digit_start, uint32_t *status, uint32_t *tile_counter, uint32_t *error)
+{
+    sort_pass_body<RB>(keys_in, vals_in, keys_out, vals_out, n, shift, digit_start, status, tile_counter, error);
+}
+
+template <int RB>
+__global__ __launch_bounds__(kSortThreads, 3) void k_sort_pass_wide(
+    const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_out, uint32_t *vals_out, size_t n,
+    int shift, const uint32_t *digit_start, uint32_t *status, uint32_t *tile_counter, uint32_t *error)
+{
+    sort_pass_body<RB>(keys_in, vals_in, keys_out, vals_out, n, shift, digit_start, status, tile_counter, error);
+}
+
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 template <int RB>
 int set_sort_attributes()
 {
     TECTO_CUDA(cudaFuncSetAttribute(k_sort_pass<RB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)pass_smem<RB>()));
+    TECTO_CUDA(cudaFuncSetAttribute(k_sort_pass_wide<RB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)pass_smem<RB>()));
     return TECTO_OK;
 }
@@ -370,7 +394,8 @@ int run_sort_rb(const SortArgs &a, const SortScratch &scr, cudaStream_t st, int 
     for (int p = 0; p < passes; ++p) {
         uint32_t *kout = a.keys[half], *vout = a.vals[half];
         uint32_t *status = scr.status + (size_t)p * tiles * R;
-        k_sort_pass<RB><<<(unsigned)tiles, kSortThreads, pass_smem<RB>(), st>>>(
+        auto pass = tiles >= kSortWideTiles ? k_sort_pass_wide<RB> : k_sort_pass<RB>;
+        pass<<<(unsigned)tiles, kSortThreads, pass_smem<RB>(), st>>>(
             kin, vin, kout, vout, a.n, RB * p, scr.hist + (size_t)p * R, status, scr.counters + p, scr.error);
         kin = kout;
         vin = vout;
