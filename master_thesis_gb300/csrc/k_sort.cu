@@ -169,8 +169,8 @@ __global__ void k_sort_scan(uint32_t *hist, int passes)
 }
 
 // One onesweep pass.  vals_in == nullptr: the value of position i is i.  Two kernels share the
-// body: k_sort_pass (the compiler takes 128 registers, two blocks per SM, no spill) for small sorts,
-// and k_sort_pass_wide (three blocks per SM, 80 registers, a few bytes of spill) once there are
+// body: k_sort_pass (the compiler takes 128 registers: two blocks per SM) for small sorts, and
+// k_sort_pass_wide (three blocks per SM: 80 registers, a few more bytes of spill) once there are
 // enough tiles to fill the extra residency.
 template <int RB>
 __device__ __forceinline__ void sort_pass_body(
