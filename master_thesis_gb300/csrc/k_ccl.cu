@@ -118,7 +118,8 @@ __device__ __forceinline__ const WorldDev *ccl_tile(const WorldDev *worlds, cons
 // edge's runs are already joined by kept ones: the components, and their minimum-index roots, are
 // those of the full edge set.  Edges whose neighbour lies in the tile only through the torus wrap
 // (a tile spanning the whole world) take the plain union.
-__global__ __launch_bounds__(256) void k_ccl_local(const WorldDev *worlds, const uint2 *tiles, int cur_id,
+// eight blocks per SM (32 registers, no spill): the pass waits on loads and shared atomics
+__global__ __launch_bounds__(256, 8) void k_ccl_local(const WorldDev *worlds, const uint2 *tiles, int cur_id,
                                                    int mode, int period)
 {
     static_assert(CX == 32 && CY % 8 == 0, "one warp per tile row, eight warps");
