@@ -164,7 +164,7 @@ __global__ __launch_bounds__(256, 8) void k_ccl_local(const WorldDev *worlds, co
             if (ax >= 0 && ax < tw && ay >= 0) {
                 nat |= 1u << k;
             } else {
-                const int nlx = wrapc(x + dxs[k], W) - x0, nly = wrapc(y + dys[k], H) - y0;
+                const int nlx = wrap_fast(x + dxs[k], W) - x0, nly = wrap_fast(y + dys[k], H) - y0;
                 if (nlx >= 0 && nlx < tw && nly >= 0 && nly < th) wrp |= 1u << k;
             }
         }
@@ -196,7 +196,7 @@ __global__ __launch_bounds__(256, 8) void k_ccl_local(const WorldDev *worlds, co
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 if (!(wrp & (1u << k))) continue;
-                const int nlx = wrapc(x + dxs[k], W) - x0, nly = wrapc(y + dys[k], H) - y0;
+                const int nlx = wrap_fast(x + dxs[k], W) - x0, nly = wrap_fast(y + dys[k], H) - y0;
                 smem_union(par, e, nly * CX + nlx);
             }
         }
@@ -235,7 +235,7 @@ __global__ __launch_bounds__(128) void k_ccl_border(const WorldDev *worlds, cons
         const unsigned m = edge_mask(id, x, y, W, H, mode);
         for (int k = 0; k < 4; ++k) {
             if (!(m & (1u << k))) continue;
-            const int nx = wrapc(x + dxs[k], W), ny = wrapc(y + dys[k], H);
+            const int nx = wrap_fast(x + dxs[k], W), ny = wrap_fast(y + dys[k], H);
             const int nlx = nx - x0, nly = ny - y0;
             if (nlx >= 0 && nlx < tw && nly >= 0 && nly < th) continue;  // handled locally
             g_union(labels, (uint32_t)((size_t)y * W + x), (uint32_t)((size_t)ny * W + nx));
