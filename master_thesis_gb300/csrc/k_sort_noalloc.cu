@@ -6,6 +6,7 @@
 // Host code cannot use the array's name as a device address, so its address is looked up with
 // cudaGetSymbolAddress once per device, with that device current, on the first call there.
 #include <mutex>
+#include <unordered_map>
 
 #include "tecto_internal.cuh"
 
@@ -23,26 +24,24 @@ constexpr size_t kScratchBytes = kSortPart + 2 * kHalf;
 
 static __device__ __align__(256) unsigned char g_sort_scratch[kScratchBytes];
 
-constexpr int kMaxDevices = 64;
 std::mutex g_mu;
-void *g_addr[kMaxDevices] = {};
+std::unordered_map<int, void *> g_addr;  // device ordinal -> address of g_sort_scratch there
 
-// Device address of g_sort_scratch on the current device (looked up once per device).
+// Device address of g_sort_scratch on the current device (looked up once per device; the address
+// stays valid for the life of the device's context, so cudaDeviceReset is not supported while the
+// library is in use).
 int scratch_address(void **out)
 {
     int dev = 0;
     TECTO_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kMaxDevices) {
-        set_error("tecto_sort_pairs_noalloc: device ordinal out of range");
-        return TECTO_ERR_UNSUPPORTED;
-    }
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_addr[dev]) {
+    auto it = g_addr.find(dev);
+    if (it == g_addr.end()) {
         void *p = nullptr;
         TECTO_CUDA(cudaGetSymbolAddress(&p, g_sort_scratch));
-        g_addr[dev] = p;
+        it = g_addr.emplace(dev, p).first;
     }
-    *out = g_addr[dev];
+    *out = it->second;
     return TECTO_OK;
 }
 

@@ -57,8 +57,9 @@ def test_noalloc_sort_matches_allocating_sort_on_two_calls_in_a_row(torch):
     stream = torch.cuda.current_stream().cuda_stream
     cap = 1 << 20  # TECTO_SORT_NOALLOC_MAX_PAIRS
     # first call: the full capacity with 32-bit keys (4 passes); second: a smaller, ragged size
-    # with 22-bit keys (3 passes) that reuses what the first call left in the shared array
-    cases = [(cap, 32, 11), (300_007, 22, 12)]
+    # with 22-bit keys (3 passes) that reuses what the first call left in the shared array;
+    # third: one pass (8-bit keys) over a ragged size whose last tile holds a single key
+    cases = [(cap, 32, 11), (300_007, 22, 12), (4097, 8, 13)]
     for n, bits, seed in cases:
         rng = np.random.default_rng(seed)
         keys = rng.integers(0, 1 << bits, n, dtype=np.uint64).astype(np.uint32)
@@ -72,6 +73,30 @@ def test_noalloc_sort_matches_allocating_sort_on_two_calls_in_a_row(torch):
         order = np.argsort(keys, kind="stable")
         np.testing.assert_array_equal(k_new, keys[order])
         np.testing.assert_array_equal(v_new, vals[order])
+
+
+def test_noalloc_sort_allocates_no_device_memory(torch):
+    """After a first call (which looks up the array's address), a call of full capacity leaves the
+    device's free memory exactly as it was."""
+    stream = torch.cuda.current_stream().cuda_stream
+    n = 1 << 20
+    rng = np.random.default_rng(21)
+    keys = rng.integers(0, 1 << 32, n, dtype=np.uint64).astype(np.uint32)
+    vals = np.arange(n, dtype=np.uint32)
+    kin, vin = _dev(torch, keys), _dev(torch, vals)
+    kout, vout = torch.empty_like(kin), torch.empty_like(vin)
+    L = T.lib()
+    T.check(L.tecto_sort_pairs_noalloc(kin.data_ptr(), vin.data_ptr(), kout.data_ptr(), vout.data_ptr(), n, 32,
+                                       stream), "tecto_sort_pairs_noalloc")
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    T.check(L.tecto_sort_pairs_noalloc(kin.data_ptr(), vin.data_ptr(), kout.data_ptr(), vout.data_ptr(), n, 32,
+                                       stream), "tecto_sort_pairs_noalloc")
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    order = np.argsort(keys, kind="stable")
+    np.testing.assert_array_equal(_host(kout), keys[order])
 
 
 def test_noalloc_sort_refuses_sizes_above_its_capacity(torch):
@@ -88,3 +113,11 @@ def test_noalloc_sort_refuses_sizes_above_its_capacity(torch):
     rc = L.tecto_sort_pairs_noalloc(kin.data_ptr(), kin.data_ptr(), kin.data_ptr(), out2.data_ptr(), 1000, 20,
                                     torch.cuda.current_stream().cuda_stream)
     assert rc == -1
+    # a good call right after the refused ones sorts correctly
+    keys = np.random.default_rng(3).integers(0, 1 << 20, 5000, dtype=np.uint32)
+    vals = np.arange(5000, dtype=np.uint32)
+    k, v = sort_noalloc(torch, _dev(torch, keys), _dev(torch, vals), 5000, 20,
+                        torch.cuda.current_stream().cuda_stream)
+    order = np.argsort(keys, kind="stable")
+    np.testing.assert_array_equal(k, keys[order])
+    np.testing.assert_array_equal(v, vals[order])
