@@ -195,15 +195,15 @@ def serve_trace(n, mean_service_s, load, seed=7, saturated=False):
 
 
 def timed_oracle(specs, seconds_cap, settings, start=0):
-    """cell-updates/s of the oracle's step alone (world generation excluded)."""
-    import master_thesis_gb300 as T
+    """cell-updates/s of the oracle's step alone (world generation excluded).  Only the oracle is
+    loaded: its own settings and generator stand in for the engine's."""
     import oracle as O
 
     cells, done, step_s, wall0 = 0, 0, 0.0, time.perf_counter()
     i = start
     while time.perf_counter() - wall0 < seconds_cap:
         W, H, P, gs, wsd = specs[i % len(specs)]
-        h, ids, pl = T.generate_world(W, H, P, 1.0, gs)
+        h, ids, pl = O.generate_world(W, H, P, 1.0, gs)
         ow = O.OracleWorld(settings, h, ids, pl, wsd)
         t1 = time.perf_counter()
         ow.step(1)
@@ -215,11 +215,11 @@ def timed_oracle(specs, seconds_cap, settings, start=0):
 
 
 def run_reference(args, ws, rank):
-    import master_thesis_gb300 as T
+    import oracle as O
 
     if rank != 0:
         return
-    s = T.baseline_settings()
+    s = O.baseline_settings()
     specs = mixed_worlds()
     cores = os.cpu_count() or 1
     # each "step" is a bounded sample of the workload: consecutive worlds of the batch, one step
@@ -262,7 +262,6 @@ def reference_gpu_lines(s):
 
         if not torch.cuda.is_available():
             return {"unavailable": "no CUDA GPU"}
-        import master_thesis_gb300 as T
         import oracle as O
     except Exception as e:  # noqa: BLE001
         return {"unavailable": f"{type(e).__name__}: {e}"}
@@ -280,8 +279,8 @@ def reference_gpu_lines(s):
     try:
         for name, W, P, vel, ccl_every in (("2048", 2048, 32, 1.0, 10), ("8192", 8192, 64, 2.0, 1)):
             try:
-                h, ids, pl = T.generate_world(W, W, P, vel, 1)
-                st = T.baseline_settings()
+                h, ids, pl = O.generate_world(W, W, P, vel, 1)
+                st = O.baseline_settings()
                 st.sim.iterationsForCCL = ccl_every
                 ms = O.ref_gpu_time(W, W, h, ids, pl, st, steps=5 if W <= 2048 else 3, warmup=2)
                 out[name] = {"value": W * W / (ms / 1e3), "unit": "cell-updates/s", "ms_per_step": ms}

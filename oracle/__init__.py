@@ -7,6 +7,7 @@ baseline and reference legs; never by the engine.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import subprocess
 from pathlib import Path
 
@@ -20,11 +21,96 @@ _o = None
 _r = None
 
 
+def reference_root() -> str:
+    """Where the reference's sources are read from: $TECTO_REFERENCE, else /root/reference."""
+    return os.environ.get("TECTO_REFERENCE", "/root/reference")
+
+
 def build(ref: bool = False) -> None:
     """make the oracle and the reference-GPU timing harness (and, with ref=True, the
-    reference-on-CPU library and the reference's device code for the GPU)."""
+    reference-on-CPU library and the reference's device code for the GPU, from the sources under
+    reference_root())."""
     targets = ["all", "harness"] + (["ref", "refgpu", "refexport"] if ref else [])
-    subprocess.run(["make", "-s", "-C", str(HERE), *targets], check=True)
+    subprocess.run(["make", "-s", "-C", str(HERE), f"REF={reference_root()}", *targets], check=True)
+
+
+# ---- the C ABI's settings and plate layouts (include/tecto.h), mirrored here so that the CPU-only
+# legs never import or load the engine; tests/test_oracle_units.py checks them against the engine's
+
+MAX_PLATES = 255
+
+_KERNEL_FLOATS_INTS = (
+    "f:inelasticCollisionMultiplierContinental f:inelasticCollisionMultiplierSubduction "
+    "f:inelasticCollisionMultiplierAccretion f:frictionCoefficientContinental f:frictionCoefficientSubduction "
+    "f:frictionCoefficientAccretion f:environmentalDragCoefficient f:velocitySmoothingFactor "
+    "f:directionSmoothingFactor f:breakScoreSmoothingFactor f:mergeDotDirectionThreshold "
+    "f:mergeVelocityDiffThreshold f:mergeMinVelocity i:mergeWaitAfterSplit i:minPlateSize "
+    "f:continentalCrustThreshold f:divergence_height_target_min f:divergence_height_target_max "
+    "f:divergence_interpolation_factor i:collisionTypeUpdateCooldown i:minCollisionSize "
+    "f:subductionOverUpliftMultiplier f:subductionUnderUpliftMultiplier f:continentalUpliftMultiplier "
+    "f:minUpliftClamp f:maxUpliftClamp i:upliftRange i:subductionOverRange i:continentalPropMaxIters "
+    "f:continentalPropThreshold f:hydrationPipeCrossSection f:hydrationPipeLength f:hydrationRainfall "
+    "f:hydrationEvaporation f:gravity f:sedimentCapacity f:sedimentErosionRate f:sedimentDepositionRate "
+    "f:pressureAccumulation f:pressureDecayRate i:pressureBlurRange f:pressureMultiplier f:curlNoiseMultiplier "
+    "f:stressSplitThreshold i:targetMinimumPlateArea i:targetMaximumPlateArea f:thermalErosionStrength "
+    "f:thermalErosionAmplitude f:thermalCellSize f:thermalThresholdAngle"
+)
+
+
+class KernelSettings(C.Structure):
+    """tecto_kernel_settings: the reference's KernelSettings, field for field."""
+    _fields_ = [(f.split(":")[1], C.c_float if f[0] == "f" else C.c_int) for f in _KERNEL_FLOATS_INTS.split()]
+
+
+class SimulationSettings(C.Structure):
+    _fields_ = [("numStartingPlates", C.c_int), ("seed", C.c_uint32), ("numVoronoiSeeds", C.c_int * 8),
+                ("numVoronoiGenerations", C.c_int), ("iterationsForCCL", C.c_int)]
+
+
+class StepSettings(C.Structure):
+    _fields_ = [("hydraulicIterations", C.c_int), ("hydraulicDt", C.c_float), ("thermalIterations", C.c_int),
+                ("upliftMode", C.c_int), ("upliftAmount", C.c_float), ("upliftSigma", C.c_float),
+                ("upliftRadius", C.c_int), ("cclConnectivity", C.c_int), ("sortRadixBits", C.c_int),
+                ("hydraulicTile", C.c_int), ("thermalTile", C.c_int), ("plateDynamics", C.c_int),
+                ("platePolicy", C.c_int), ("reserved", C.c_int * 3)]
+
+
+class Settings(C.Structure):
+    _fields_ = [("kernel", KernelSettings), ("sim", SimulationSettings), ("step", StepSettings)]
+
+
+PLATE_DTYPE = np.dtype([("velocity", "<f4"), ("direction_x", "<f4"), ("direction_y", "<f4"),
+                        ("pixelCenter_x", "<f4"), ("pixelCenter_y", "<f4")])
+PLATE_DYNAMICS_DTYPE = np.dtype(
+    [("velocitySmoothed", "<f4"), ("directionSmoothed_x", "<f4"), ("directionSmoothed_y", "<f4"),
+     ("geometricCenter_x", "<f4"), ("geometricCenter_y", "<f4"), ("mass", "<f4"), ("size", "<i4"),
+     ("mergeWaitTime", "<i4"), ("frictionLoss", "<f4")]
+)
+
+
+def default_settings() -> Settings:
+    """The reference's defaults (or_settings_default)."""
+    s = Settings()
+    lib().or_settings_default(C.addressof(s))
+    return s
+
+
+def baseline_settings() -> Settings:
+    """The benchmark physics on the reference's parameters (or_settings_baseline)."""
+    s = Settings()
+    lib().or_settings_baseline(C.addressof(s))
+    return s
+
+
+def generate_world(W: int, H: int, plates: int, vel_range: float, gen_seed: int):
+    """The benchmark's synthetic world (or_generate_world): (height f32[H,W], plate id u8[H,W],
+    plates[255])."""
+    h = np.empty((H, W), np.float32)
+    ids = np.empty((H, W), np.uint8)
+    pl = np.zeros(MAX_PLATES, PLATE_DTYPE)
+    if lib().or_generate_world(W, H, plates, vel_range, gen_seed, h.ctypes.data, ids.ctypes.data, pl.ctypes.data):
+        raise ValueError("or_generate_world: invalid size or plate count (1..255)")
+    return h, ids, pl
 
 
 REF_CUBIN = HERE / "_ref" / "ref_kernels.cubin"
@@ -141,6 +227,9 @@ def lib() -> C.CDLL:
         L.or_sinf.argtypes = [C.c_float]
         L.or_sinf.restype = C.c_float
         L.or_gaussian_weights.argtypes = [C.c_float, C.c_int, V]
+        L.or_settings_default.argtypes = [V]
+        L.or_settings_baseline.argtypes = [V]
+        L.or_generate_world.argtypes = [C.c_int, C.c_int, C.c_int, C.c_float, C.c_uint64, V, V, V]
         L.or_use_libm_sin.argtypes = [C.c_int]
         _o = L
     return _o
@@ -258,7 +347,6 @@ def log10f(x: float) -> float:
 
 def reference_seeds(W, H, seed, num_plates, gens):
     """or_reference_seeds: (x, y, id) of the seeds, plate records, plate dynamics records."""
-    from master_thesis_gb300 import MAX_PLATES, PLATE_DTYPE, PLATE_DYNAMICS_DTYPE
     g = np.ascontiguousarray(gens, np.int32)
     cap = max([num_plates] + [int(v) for v in g])
     sx, sy = np.zeros(cap, np.float32), np.zeros(cap, np.float32)
@@ -301,7 +389,6 @@ def merge(ids, plates, dyn, bitmap, settings):
 
 def plate_stats(h, ids, iteration, dyn=None):
     """or_plate_stats: mass, size and geometric centre per plate (updates a copy of dyn)."""
-    from master_thesis_gb300 import MAX_PLATES, PLATE_DYNAMICS_DTYPE
     H, W = h.shape
     out = np.zeros(MAX_PLATES, PLATE_DYNAMICS_DTYPE) if dyn is None else dyn.copy()
     lib().or_plate_stats(W, H, _P(np.ascontiguousarray(h, np.float32)), _P(np.ascontiguousarray(ids, np.uint8)),
@@ -390,7 +477,6 @@ class OracleWorld:
         self.seed = seed
         self.iteration = C.c_uint32(0)
 
-        from master_thesis_gb300 import MAX_PLATES, PLATE_DYNAMICS_DTYPE
         self.dyn = np.zeros(MAX_PLATES, PLATE_DYNAMICS_DTYPE)
         self.pressure = None
 

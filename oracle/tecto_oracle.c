@@ -1573,3 +1573,183 @@ int or_merge(int W, int H, uint8_t *id, const tecto_plate *plates, const tecto_p
         if (id[i] != NPLATE && merge_ids[id[i]] > 0) id[i] = (uint8_t)((int)NPLATE - merge_ids[id[i]]);
     return merges;
 }
+
+/* ---- settings and the synthetic world generator, restated for the CPU-only legs ----------------
+ *
+ * The reference arm and the CPU baseline of bench.py must not load the engine's library, so the
+ * oracle carries its own copies of the two parameter sets and of the benchmark's world generator.
+ * tests/test_oracle_units.py checks that both equal the engine's byte for byte. */
+
+/* KernelSettings' initialisers (src/cuda_compute/kernel_settings.cuh:6-71), SimulationSettings'
+ * (src/generation_settings.h:69-72) and the literal step constants of plate_tectonic_sim.cu:73,
+ * :336-363. */
+void or_settings_default(tecto_settings *out)
+{
+    memset(out, 0, sizeof(*out));
+    tecto_kernel_settings *k = &out->kernel;
+    k->inelasticCollisionMultiplierContinental = 1.f;
+    k->inelasticCollisionMultiplierSubduction = 0.25f;
+    k->inelasticCollisionMultiplierAccretion = 0.5f;
+    k->frictionCoefficientContinental = 1.f;
+    k->frictionCoefficientSubduction = 0.2f;
+    k->frictionCoefficientAccretion = 0.5f;
+    k->environmentalDragCoefficient = 0.25f;
+    k->velocitySmoothingFactor = 0.9f;
+    k->directionSmoothingFactor = 0.9f;
+    k->breakScoreSmoothingFactor = 0.9f;
+    k->mergeDotDirectionThreshold = .998f;
+    k->mergeVelocityDiffThreshold = 0.01f;
+    k->mergeMinVelocity = 0.05f;
+    k->mergeWaitAfterSplit = 10;
+    k->minPlateSize = 10;
+    k->continentalCrustThreshold = 10000.f;
+    k->divergence_height_target_min = 1000.f;
+    k->divergence_height_target_max = 2000.f;
+    k->divergence_interpolation_factor = 0.025f;
+    k->collisionTypeUpdateCooldown = 4;
+    k->minCollisionSize = 50;
+    k->subductionOverUpliftMultiplier = 0.005f;
+    k->subductionUnderUpliftMultiplier = 0.01f;
+    k->continentalUpliftMultiplier = 0.01f;
+    k->minUpliftClamp = 0.f;
+    k->maxUpliftClamp = 20000.f;
+    k->upliftRange = 50;
+    k->subductionOverRange = 20;
+    k->continentalPropMaxIters = 50;
+    k->continentalPropThreshold = 13000;
+    k->hydrationPipeCrossSection = 1000;
+    k->hydrationPipeLength = 1000;
+    k->hydrationRainfall = (float)0.101;
+    k->hydrationEvaporation = (float)0.303;
+    k->gravity = (float)9.81;
+    k->sedimentCapacity = (float)0.9;
+    k->sedimentErosionRate = (float)0.5;
+    k->sedimentDepositionRate = (float)0.01;
+    k->pressureAccumulation = 0.02f;
+    k->pressureDecayRate = 0.8f;
+    k->pressureBlurRange = 25;
+    k->pressureMultiplier = 1.0f;
+    k->curlNoiseMultiplier = 30.f;
+    k->stressSplitThreshold = 30.0f;
+    k->targetMinimumPlateArea = 100;
+    k->targetMaximumPlateArea = 100000;
+    k->thermalErosionStrength = 1.0f;
+    k->thermalErosionAmplitude = 0.5f;
+    k->thermalCellSize = 1000.0f;
+    k->thermalThresholdAngle = 0.5f;
+    out->sim.numStartingPlates = 16;
+    out->sim.seed = 1000;
+    out->sim.numVoronoiSeeds[0] = 200;
+    out->sim.numVoronoiSeeds[1] = 500;
+    out->sim.numVoronoiGenerations = 2;
+    out->sim.iterationsForCCL = 10;
+    out->step.hydraulicIterations = 10;
+    out->step.hydraulicDt = 1.0f;
+    out->step.thermalIterations = 1;
+    out->step.upliftMode = TECTO_UPLIFT_GAUSSIAN;
+    out->step.upliftAmount = 0.01f;
+    out->step.upliftSigma = 1.5f;
+    out->step.upliftRadius = 3;
+    out->step.cclConnectivity = TECTO_CCL_REF8;
+}
+
+/* The benchmark physics mapped onto the reference's parameters: rain 0.01, evaporation 0.05,
+ * Kc 0.1, Ks 0.3, Kd 0.1, 20 hydraulic sub-iterations of dt 0.02, 10 thermal iterations with talus
+ * 0.01 and rate 0.5, continental above height 0, Gaussian uplift 0.01 (sigma 1.5, radius 3), 4-connected
+ * CCL every 10 steps. */
+void or_settings_baseline(tecto_settings *out)
+{
+    or_settings_default(out);
+    tecto_kernel_settings *k = &out->kernel;
+    k->hydrationRainfall = 0.01f;
+    k->hydrationEvaporation = 0.05f;
+    k->sedimentCapacity = 0.1f;
+    k->sedimentErosionRate = 0.3f;
+    k->sedimentDepositionRate = 0.1f;
+    k->thermalThresholdAngle = 0.01f;
+    k->thermalCellSize = 1.0f;
+    k->thermalErosionAmplitude = 0.5f;
+    k->thermalErosionStrength = 1.0f;
+    k->continentalCrustThreshold = 0.0f;
+    out->step.hydraulicIterations = 20;
+    out->step.hydraulicDt = 0.02f;
+    out->step.thermalIterations = 10;
+    out->step.upliftMode = TECTO_UPLIFT_GAUSSIAN;
+    out->step.upliftAmount = 0.01f;
+    out->step.upliftSigma = 1.5f;
+    out->step.upliftRadius = 3;
+    out->step.cclConnectivity = TECTO_CCL_4;
+    out->sim.iterationsForCCL = 10;
+}
+
+/* splitmix64 (G. L. Steele, D. Lea, C. H. Flood, "Fast splittable pseudorandom number generators",
+ * OOPSLA 2014) and a 24-bit uniform in [0, 1). */
+static uint64_t or_splitmix64(uint64_t *s)
+{
+    uint64_t z = (*s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+static float or_u01(uint64_t r) { return (float)(r >> 40) * (1.0f / 16777216.0f); }
+
+/* The synthetic world of the benchmark configurations: P seed points uniform on the grid, each a
+ * plate with a velocity uniform in [-velRange, velRange]^2; every cell takes the plate of its
+ * nearest seed on the torus (first on ties); even plates are continental, 0.5 + 0.05 N, odd ones
+ * oceanic, -0.5 + 0.02 N, N the Irwin-Hall sum of 12 uniforms minus 6 from a per-cell stream. */
+int or_generate_world(int W, int H, int P, float velRange, uint64_t genSeed, float *height_out, uint8_t *id_out,
+                      tecto_plate *plates_out)
+{
+    if (W < 1 || H < 1 || P < 1 || P > TECTO_MAX_PLATES) return -1;
+    float *sx = (float *)calloc((size_t)P, sizeof(float)), *sy = (float *)calloc((size_t)P, sizeof(float));
+    if (!sx || !sy) {
+        free(sx);
+        free(sy);
+        return -3;
+    }
+    uint64_t st = genSeed;
+    if (plates_out) memset(plates_out, 0, sizeof(tecto_plate) * TECTO_MAX_PLATES);
+    for (int k = 0; k < P; ++k) {
+        sx[k] = or_u01(or_splitmix64(&st)) * (float)W;
+        sy[k] = or_u01(or_splitmix64(&st)) * (float)H;
+        const float vx = (2.0f * or_u01(or_splitmix64(&st)) - 1.0f) * velRange;
+        const float vy = (2.0f * or_u01(or_splitmix64(&st)) - 1.0f) * velRange;
+        const float v = sqrtf(vx * vx + vy * vy);
+        if (plates_out) {
+            plates_out[k].velocity = v;
+            plates_out[k].direction_x = v > 0.0f ? vx / v : 1.0f;
+            plates_out[k].direction_y = v > 0.0f ? vy / v : 0.0f;
+            plates_out[k].pixelCenter_x = sx[k] - floorf(sx[k]);
+            plates_out[k].pixelCenter_y = sy[k] - floorf(sy[k]);
+        }
+    }
+    const float fW = (float)W, fH = (float)H;
+#pragma omp parallel for schedule(static)
+    for (int y = 0; y < H; ++y) {
+        for (int x = 0; x < W; ++x) {
+            const size_t i = (size_t)y * (size_t)W + (size_t)x;
+            float best = 3.4e38f;
+            int bid = 0;
+            for (int k = 0; k < P; ++k) {
+                const float dx = fabsf((float)x - sx[k]), dy = fabsf((float)y - sy[k]);
+                const float wx = fminf(dx, fW - dx), wy = fminf(dy, fH - dy);
+                const float d2 = wx * wx + wy * wy;
+                if (d2 < best) {
+                    best = d2;
+                    bid = k;
+                }
+            }
+            if (id_out) id_out[i] = (uint8_t)bid;
+            if (height_out) {
+                uint64_t cs = genSeed ^ (0xD1B54A32D192ED03ull * (uint64_t)(i + 1));
+                float sum = 0.0f;
+                for (int r = 0; r < 12; ++r) sum = sum + or_u01(or_splitmix64(&cs));
+                const float n = sum - 6.0f;
+                height_out[i] = (bid % 2 == 0) ? 0.5f + 0.05f * n : -0.5f + 0.02f * n;
+            }
+        }
+    }
+    free(sx);
+    free(sy);
+    return 0;
+}

@@ -130,6 +130,14 @@ void or_gaussian_weights(float sigma, int radius, float *w_out);
 float or_sinf(float x);
 void or_use_libm_sin(int on);
 
+/* The reference's default parameters and the benchmark's mapping of them (the same values as
+ * tecto_settings_default / tecto_settings_baseline), and the benchmark's synthetic world generator
+ * (the same worlds as tecto_generate_world_host), for the legs that must not load the engine. */
+void or_settings_default(tecto_settings *out);
+void or_settings_baseline(tecto_settings *out);
+int or_generate_world(int W, int H, int P, float velRange, uint64_t genSeed, float *height_out, uint8_t *id_out,
+                      tecto_plate *plates_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,6 +1,7 @@
 """Unit properties of the oracle's building blocks (CPU)."""
 from __future__ import annotations
 
+import ctypes as C
 import math
 
 import numpy as np
@@ -81,3 +82,26 @@ def test_gaussian_uplift_against_numpy_convolution(sigma, radius):
         out += wgt * np.roll(blur, -d, axis=0)
     assert (word > 0xFF).sum() > 10
     np.testing.assert_allclose(hg.astype(np.float64) - hn.astype(np.float64), out, atol=2e-6, rtol=0)
+
+
+def test_oracle_settings_and_layouts_equal_the_engines():
+    """The CPU legs of bench.py use the oracle's copies of the settings, the struct layouts and the
+    synthetic generator, so that they never load the engine; they must be the engine's exactly."""
+    for name in ("KernelSettings", "SimulationSettings", "StepSettings", "Settings"):
+        a, b = getattr(O, name), getattr(T, name)
+        assert C.sizeof(a) == C.sizeof(b), name
+        assert [(f, getattr(a, f).offset) for f, _ in a._fields_] == [(f, getattr(b, f).offset) for f, _ in b._fields_]
+    assert O.PLATE_DTYPE == T.PLATE_DTYPE and O.PLATE_DYNAMICS_DTYPE == T.PLATE_DYNAMICS_DTYPE
+    assert O.MAX_PLATES == T.MAX_PLATES
+    assert bytes(O.default_settings()) == bytes(T.default_settings())
+    assert bytes(O.baseline_settings()) == bytes(T.baseline_settings())
+
+
+@pytest.mark.parametrize("W,H,P,vel,seed", [(1, 1, 1, 1.0, 0), (96, 64, 8, 1.0, 6), (257, 130, 32, 2.0, 12345),
+                                            (64, 3, 255, 0.5, 2**63 + 7)])
+def test_oracle_generator_equals_the_engines(W, H, P, vel, seed):
+    ho, io, po = O.generate_world(W, H, P, vel, seed)
+    he, ie, pe = T.generate_world(W, H, P, vel, seed)
+    np.testing.assert_array_equal(ho, he)
+    np.testing.assert_array_equal(io, ie)
+    np.testing.assert_array_equal(po.view(np.uint8), pe.view(np.uint8))
