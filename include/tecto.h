@@ -135,7 +135,9 @@ typedef struct tecto_step_settings {
     int sortRadixBits;        /* collision sort digit width 8..11; 0 = autotuner's choice, else 8 */
     int hydraulicTile;        /* 0 = autotuner's choice, else 4; 1: 64x16/256 threads, 2: 64x32/256,
                                  3: 64x32/512, 4: 64x32/1024, 5: 64x64/1024, 6: 64x16/512 (3 blocks
-                                 per SM), 7: 64x16/384 (4 blocks per SM) */
+                                 per SM), 7: 64x16/384 (4 blocks per SM), 8: column strips of 56
+                                 cells marched down by one warp each, no block barriers (the split
+                                 path, 50 dt >= 1.5, runs variant 4) */
     int thermalTile;          /* 0 = autotuner's choice, else 4; 1: 64x32 tiles / 1024 threads, up to 5
                                  iterations per launch; 2: 64x16 / 512, 2 blocks per SM, up to 4;
                                  3: 64x16 / 768, 2 blocks per SM, up to 3; 4: 64x16 / 512, 3 blocks
@@ -328,6 +330,19 @@ int tecto_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t 
                      uint32_t *vals_out, size_t n, int key_bits, void *scratch,
                      size_t scratch_bytes, tecto_stream_t stream);
 
+/* The same sort with the digit width chosen by the caller: radix_bits 8..11 (0 = 8), the widths
+ * the collision sort's autotuner picks from (tecto_step_settings::sortRadixBits).  Scratch must
+ * hold tecto_sort_scratch_bytes_radix(n, key_bits, radix_bits) bytes; other widths are
+ * TECTO_ERR_INVALID (and 0 scratch bytes). */
+size_t tecto_sort_scratch_bytes_radix(size_t n, int key_bits, int radix_bits);
+int tecto_sort_pairs_radix(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_out,
+                           uint32_t *vals_out, size_t n, int key_bits, int radix_bits, void *scratch,
+                           size_t scratch_bytes, tecto_stream_t stream);
+/* 1 when a sort of n pairs runs its passes in the form for large sorts (from 4096 tiles of 4096
+ * keys, i.e. 16 777 216 pairs: three blocks per SM), 0 when it runs the form for smaller sorts.
+ * The collision sort of a batch or world uses the same rule on its cell count. */
+int tecto_sort_wide_pass(size_t n);
+
 /* The same stable sort for callers that cannot allocate device memory: it needs no scratch
  * argument and makes no allocation of any kind (no cudaMalloc, cudaFree or allocating library
  * call).  This entry point has no counterpart in the reference.  Who needs it: a host that hands
@@ -340,12 +355,14 @@ int tecto_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t 
  * and rules:
  *  - n > TECTO_SORT_NOALLOC_MAX_PAIRS is rejected with TECTO_ERR_INVALID (nothing runs);
  *  - outputs must not alias the inputs (TECTO_ERR_INVALID);
- *  - the first call on each device resolves the array's device address with that device current;
- *    make that first call before any stream capture;
+ *  - the first call on each device resolves the array's device address with that device current
+ *    and keeps it for the life of that device's context; make that first call before any stream
+ *    capture begins, and do not reset the device (cudaDeviceReset) while the library is in use;
  *  - all calls share the one array: two calls whose work overlaps on the GPU (different streams,
  *    or different host threads on the same device) race and corrupt each other's results, so
  *    serialise them.  Each call clears the parts that must start at zero itself.
- * Synchronous: returns after the result is in keys_out/vals_out. */
+ * Every call is synchronous: it reads the sort's error word back to the host and waits for the
+ * stream, so it returns only after the result is in keys_out/vals_out. */
 #define TECTO_SORT_NOALLOC_MAX_PAIRS ((size_t)1 << 20)
 int tecto_sort_pairs_noalloc(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_out,
                              uint32_t *vals_out, size_t n, int key_bits, tecto_stream_t stream);
@@ -356,8 +373,10 @@ int tecto_sort_pairs_noalloc(const uint32_t *keys_in, const uint32_t *vals_in, u
  * advances all its worlds together: every phase is one kernel launch over a work list of
  * (world, tile) items, the sort runs once over all the batch's cells, and a step is replayed as
  * one CUDA graph.  Worlds keep their own device state and keep it between steps; results are
- * identical to stepping each world alone.  All worlds of a batch share one settings struct and one
- * device.  While a world is in a batch, tecto_world_step and the phase calls refuse it. */
+ * identical to stepping each world alone.  All worlds of a batch share one device and the settings
+ * a step reads (kernel and step settings, the CCL period); the initialisation-only fields of
+ * SimulationSettings (plate count, seed, Voronoi generations) may differ.  While a world is in a
+ * batch, tecto_world_step and the phase calls refuse it. */
 typedef struct tecto_batch tecto_batch;
 int tecto_batch_create(tecto_batch **out);
 int tecto_batch_destroy(tecto_batch *batch);  /* worlds stay alive and leave the batch */
@@ -405,10 +424,10 @@ int tecto_batch_phase_thermal(tecto_batch *batch, int iterations, tecto_stream_t
  * the nearest tuned class on their device, else the defaults (hydraulic variant 4, thermal
  * variant 4, 8-bit digits). */
 typedef struct tecto_tuning {
-    int hydraulicTile;       /* chosen variant, 1..7 */
+    int hydraulicTile;       /* chosen variant, 1..8 */
     int sortRadixBits;       /* chosen digit width, 8..11 */
     int thermalTile;         /* chosen variant, 1..4 */
-    float hydraulic_ms[7];   /* one hydraulic sub-iteration with variant 1..7 */
+    float hydraulic_ms[8];   /* one hydraulic sub-iteration with variant 1..8 */
     float sort_ms[4];        /* the collision sort with 8..11-bit digits */
     float thermal_ms[4];     /* ten thermal iterations with variant 1..4 */
 } tecto_tuning;

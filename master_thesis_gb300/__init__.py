@@ -184,7 +184,7 @@ class Tuning(C.Structure):
     """tecto_tuning: the autotuner's choice and the per-candidate timings."""
     _fields_ = [
         ("hydraulicTile", C.c_int), ("sortRadixBits", C.c_int), ("thermalTile", C.c_int),
-        ("hydraulic_ms", C.c_float * 7), ("sort_ms", C.c_float * 4), ("thermal_ms", C.c_float * 4),
+        ("hydraulic_ms", C.c_float * 8), ("sort_ms", C.c_float * 4), ("thermal_ms", C.c_float * 4),
     ]
 
     def as_dict(self) -> dict:
@@ -251,6 +251,9 @@ def _declare(L: C.CDLL) -> None:
         "tecto_phase_ccl": ([P, C.c_int, P], C.c_int),
         "tecto_sort_scratch_bytes": ([C.c_size_t, C.c_int], C.c_size_t),
         "tecto_sort_pairs": ([P, P, P, P, C.c_size_t, C.c_int, P, C.c_size_t, P], C.c_int),
+        "tecto_sort_scratch_bytes_radix": ([C.c_size_t, C.c_int, C.c_int], C.c_size_t),
+        "tecto_sort_pairs_radix": ([P, P, P, P, C.c_size_t, C.c_int, C.c_int, P, C.c_size_t, P], C.c_int),
+        "tecto_sort_wide_pass": ([C.c_size_t], C.c_int),
         "tecto_sort_pairs_noalloc": ([P, P, P, P, C.c_size_t, C.c_int, P], C.c_int),
         "tecto_world_check": ([P, P], C.c_int),
         "tecto_world_launch_count": ([P, C.POINTER(C.c_uint64)], C.c_int),

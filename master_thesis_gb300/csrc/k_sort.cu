@@ -485,32 +485,47 @@ int run_sort(const SortArgs &a, const SortScratch &scr, cudaStream_t st, int *re
 
 // ---- C ABI: standalone sort -------------------------------------------------------------------
 
-extern "C" size_t tecto_sort_scratch_bytes(size_t n, int key_bits)
+extern "C" size_t tecto_sort_scratch_bytes_radix(size_t n, int key_bits, int radix_bits)
 {
     if (key_bits < 1 || key_bits > 32) return 0;
+    if (radix_bits == 0) radix_bits = 8;
+    if (!tecto::valid_radix_bits(radix_bits)) return 0;
     // two ping-pong halves for keys and values are carved after the sort's own scratch
-    return tecto::sort_scratch_bytes(n, key_bits, 8) + 4 * tecto::align256(n * sizeof(uint32_t));
+    return tecto::sort_scratch_bytes(n, key_bits, radix_bits) + 4 * tecto::align256(n * sizeof(uint32_t));
 }
 
-extern "C" int tecto_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_out,
-                                uint32_t *vals_out, size_t n, int key_bits, void *scratch,
-                                size_t scratch_bytes, tecto_stream_t stream)
+extern "C" size_t tecto_sort_scratch_bytes(size_t n, int key_bits)
+{
+    return tecto_sort_scratch_bytes_radix(n, key_bits, 8);
+}
+
+extern "C" int tecto_sort_wide_pass(size_t n)
+{
+    return (n + tecto::kSortTile - 1) / tecto::kSortTile >= (size_t)tecto::kSortWideTiles ? 1 : 0;
+}
+
+extern "C" int tecto_sort_pairs_radix(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_out,
+                                      uint32_t *vals_out, size_t n, int key_bits, int radix_bits, void *scratch,
+                                      size_t scratch_bytes, tecto_stream_t stream)
 {
     using namespace tecto;
     if (n == 0) return TECTO_OK;
+    if (radix_bits == 0) radix_bits = 8;
     if (!keys_in || !vals_in || !keys_out || !vals_out || !scratch || key_bits < 1 ||
-        key_bits > 32 || n > (size_t)kValueMask) {
+        key_bits > 32 || n > (size_t)kValueMask || !valid_radix_bits(radix_bits)) {
         set_error("tecto_sort_pairs: invalid argument");
         return TECTO_ERR_INVALID;
     }
-    if (scratch_bytes < tecto_sort_scratch_bytes(n, key_bits)) {
+    if (scratch_bytes < tecto_sort_scratch_bytes_radix(n, key_bits, radix_bits)) {
         set_error("tecto_sort_pairs: scratch too small");
         return TECTO_ERR_INVALID;
     }
+    int rc;
+    if (radix_bits > 8 && (rc = sort_kernel_attributes()) != TECTO_OK) return rc;
     cudaStream_t st = (cudaStream_t)stream;
     SortScratch scr{};
-    sort_scratch_carve(scratch, n, key_bits, 8, &scr);
-    char *p = (char *)scratch + sort_scratch_bytes(n, key_bits, 8);
+    sort_scratch_carve(scratch, n, key_bits, radix_bits, &scr);
+    char *p = (char *)scratch + sort_scratch_bytes(n, key_bits, radix_bits);
     const size_t arr = align256(n * sizeof(uint32_t));
     SortArgs a{};
     a.keys_in = keys_in;
@@ -523,7 +538,7 @@ extern "C" int tecto_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in
     a.key_bits = key_bits;
     TECTO_CUDA(cudaMemsetAsync(scr.error, 0, 4, st));
     int half = 0;
-    const int rc = run_sort(a, scr, st, &half);
+    rc = run_sort(a, scr, st, &half);
     if (rc != TECTO_OK) return rc;
     TECTO_CUDA(cudaMemcpyAsync(keys_out, a.keys[half], n * 4, cudaMemcpyDeviceToDevice, st));
     TECTO_CUDA(cudaMemcpyAsync(vals_out, a.vals[half], n * 4, cudaMemcpyDeviceToDevice, st));
@@ -535,4 +550,12 @@ extern "C" int tecto_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in
         return TECTO_ERR_DEVICE_TIMEOUT;
     }
     return TECTO_OK;
+}
+
+extern "C" int tecto_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_out,
+                                uint32_t *vals_out, size_t n, int key_bits, void *scratch,
+                                size_t scratch_bytes, tecto_stream_t stream)
+{
+    return tecto_sort_pairs_radix(keys_in, vals_in, keys_out, vals_out, n, key_bits, 8, scratch, scratch_bytes,
+                                  stream);
 }

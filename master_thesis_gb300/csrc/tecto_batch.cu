@@ -34,6 +34,25 @@ void build_tiles(const Batch &b, int kind, std::vector<uint2> &out)
     }
 }
 
+}  // namespace
+
+void build_strips(const Batch &b, std::vector<uint4> &out, unsigned long long *rows)
+{
+    out.clear();
+    unsigned long long r = 0;
+    for (size_t wi = 0; wi < b.members.size(); ++wi) {
+        const tecto_world *w = b.members[wi];
+        for (int x0 = 0; x0 < w->W; x0 += kStripInner) {
+            const int iw = std::min(kStripInner, w->W - x0);
+            out.push_back(make_uint4((unsigned)wi, (unsigned)x0, (unsigned)iw, (unsigned)r));
+            r += (unsigned long long)w->H;
+        }
+    }
+    *rows = r;
+}
+
+namespace {
+
 // Copy the state of group `g` (0 height, 1 water/sediment/flux, 2 plate ids) of world w into
 // ping-pong half `to`.
 int move_half(tecto_world *w, int g, int to, cudaStream_t st)
@@ -50,6 +69,15 @@ int move_half(tecto_world *w, int g, int to, cudaStream_t st)
         TECTO_CUDA(cudaMemcpyAsync(w->dev.id[to], w->dev.id[from], N, cudaMemcpyDeviceToDevice, st));
     }
     return TECTO_OK;
+}
+
+// Whether two worlds step alike: every parameter a step reads (the kernel and step settings and the
+// CCL period).  The rest of SimulationSettings (plate count, seed, Voronoi generations) is read by
+// the initialisation only, so worlds initialised differently may share a batch.
+bool same_step_settings(const tecto_settings &a, const tecto_settings &b)
+{
+    return std::memcmp(&a.kernel, &b.kernel, sizeof(a.kernel)) == 0 &&
+           std::memcmp(&a.step, &b.step, sizeof(a.step)) == 0 && a.sim.iterationsForCCL == b.sim.iterationsForCCL;
 }
 
 }  // namespace
@@ -69,8 +97,8 @@ int batch_join(Batch &b, tecto_world *w, cudaStream_t st)
         b.cur_wsf = w->cur_wsf;
         b.cur_id = w->cur_id;
     } else {
-        if (std::memcmp(&b.settings, &w->settings, sizeof(tecto_settings)) != 0) {
-            set_error("all worlds of a batch must share the same settings");
+        if (!same_step_settings(b.settings, w->settings)) {
+            set_error("all worlds of a batch must share the same step settings");
             return TECTO_ERR_INVALID;
         }
         if (w->device != b.device) {
@@ -194,6 +222,10 @@ int batch_prepare(Batch &b, cudaStream_t st)
         b.ntiles[k] = (int)tiles[k].size();
         need += a256(tiles[k].size() * sizeof(uint2));
     }
+    std::vector<uint4> strips;
+    build_strips(b, strips, &b.strip_rows);
+    b.nstrips = (int)strips.size();
+    need += a256(strips.size() * sizeof(uint4));
     if (need > b.table_bytes) {
         if (b.table_arena) cudaFree(b.table_arena);
         b.table_arena = nullptr;
@@ -210,11 +242,15 @@ int batch_prepare(Batch &b, cudaStream_t st)
         b.d_tiles[k] = (uint2 *)p;
         p += a256(tiles[k].size() * sizeof(uint2));
     }
+    b.d_strips = (uint4 *)p;
+    p += a256(strips.size() * sizeof(uint4));
     TECTO_CUDA(cudaMemcpyAsync(b.d_worlds, table.data(), n * sizeof(WorldDev), cudaMemcpyHostToDevice, st));
     TECTO_CUDA(cudaMemcpyAsync(b.d_vbase, vbase.data(), (n + 1) * 4, cudaMemcpyHostToDevice, st));
     for (int k = 0; k < TK_COUNT; ++k)
         TECTO_CUDA(cudaMemcpyAsync(b.d_tiles[k], tiles[k].data(), tiles[k].size() * sizeof(uint2),
                                    cudaMemcpyHostToDevice, st));
+    TECTO_CUDA(cudaMemcpyAsync(b.d_strips, strips.data(), strips.size() * sizeof(uint4), cudaMemcpyHostToDevice,
+                               st));
     // batch-level buffers: key/value ping-pong for `capacity` cells, the control block, then the
     // sort scratch of the current size and digit width
     const int kb = key_bits_for(total);

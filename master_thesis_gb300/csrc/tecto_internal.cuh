@@ -183,6 +183,11 @@ struct Batch {
     uint32_t *d_vbase = nullptr;             // [n + 1] ascending virtual bases, last = total
     uint2 *d_tiles[TK_COUNT] = {};           // (world, ty << 16 | tx)
     int ntiles[TK_COUNT] = {};
+    // column strips of the marching hydraulic kernel (hydraulic variant kHydroStripVariant):
+    // {world, first column, interior width, first strip-row}, strip-rows counted over all strips
+    uint4 *d_strips = nullptr;
+    int nstrips = 0;
+    unsigned long long strip_rows = 0;
     void *table_arena = nullptr;
     size_t table_bytes = 0;
     // batch-level buffers, sized for `capacity` cells
@@ -332,8 +337,12 @@ void gaussian_weights(float sigma, int radius, float *out);
 int ensure_kernel_attributes();
 int hydro_variant_for(const tecto_settings &s);  // 0 when the settings leave the choice open
 constexpr int kDefaultRadixBits = 8;
-constexpr int kHydroVariantCount = 7;
+constexpr int kHydroVariantCount = 8;
 constexpr int kDefaultHydroVariant = 4;          // 64 x 32 cells, 1024 threads
+constexpr int kHydroStripVariant = 8;            // marching column strips (fused path only)
+constexpr int kStripInner = 56;                  // interior columns of one strip (64 with the halo)
+// the strip table of a batch: every member's columns cut into strips of kStripInner
+void build_strips(const Batch &b, std::vector<uint4> &out, unsigned long long *rows);
 constexpr int kThermalVariantCount = 4;
 constexpr int kDefaultThermalVariant = 4;        // 64 x 16 cells, 512 threads, 2 iterations per launch
 int thermal_variant_for(const tecto_settings &s);  // 0 when the settings leave the choice open

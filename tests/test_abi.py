@@ -121,4 +121,11 @@ def test_invalid_arguments_are_rejected_without_touching_a_gpu():
     assert L.tecto_sort_pairs(None, None, None, None, 10, 8, None, 0, None) == -1
     assert L.tecto_sort_scratch_bytes(100, 0) == 0 and L.tecto_sort_scratch_bytes(100, 33) == 0
     assert L.tecto_sort_scratch_bytes(1 << 20, 20) > 4 * (1 << 22)
+    assert L.tecto_sort_pairs_radix(None, None, None, None, 10, 8, 11, None, 0, None) == -1
+    assert L.tecto_sort_scratch_bytes_radix(100, 20, 7) == 0 and L.tecto_sort_scratch_bytes_radix(100, 20, 12) == 0
+    assert L.tecto_sort_scratch_bytes_radix(1 << 20, 20, 0) == L.tecto_sort_scratch_bytes(1 << 20, 20)
+    assert L.tecto_sort_scratch_bytes_radix(1 << 20, 20, 11) > L.tecto_sort_scratch_bytes(1 << 20, 20)
+    # the pass form for large sorts starts at 4096 tiles of 4096 keys
+    assert L.tecto_sort_wide_pass(4096 * 4096) == 1 and L.tecto_sort_wide_pass(4096 * 4096 - 4096) == 0
+    assert L.tecto_sort_wide_pass(4095 * 4096 + 1) == 1
     assert L.tecto_world_destroy(None) == 0

@@ -67,17 +67,19 @@ def test_initialised_world_steps_like_the_oracle(stream):
         np.testing.assert_array_equal(w.download(T.FIELD_HEIGHT, stream), o.h, err_msg=f"heights step {step}")
 
 
-def test_server_admits_reference_initialised_worlds(stream):
+@pytest.mark.parametrize("spacing", [0.0, 0.001])
+def test_server_admits_reference_initialised_worlds(stream, spacing):
     """Served requests initialised with the reference's initialisation give the same worlds as
-    initialising and stepping them directly."""
+    initialising and stepping them directly.  Each request has its own plate count, a field the
+    initialisation alone reads; with all arrivals at t = 0 the three worlds share the batch."""
     s = settings(1, (40,))
     reqs = [T.Request(width=W, height=H, plates=p, steps=st, velRange=1.0, genSeed=0, worldSeed=500 + i,
-                      arrival_s=0.001 * i)
+                      arrival_s=spacing * i)
             for i, (W, H, p, st) in enumerate([(64, 64, 6, 3), (96, 48, 4, 2), (80, 80, 9, 4)])]
     sv = T.Server(s, 3 * T.world_bytes(96, 80), max_worlds=3)
     sv.set_init(T.SERVER_INIT_REFERENCE)
     res, st = sv.run_trace(reqs, stream)
-    assert st.completed == 3
+    assert st.completed == 3, [(r.status, r.admit_s, r.finish_s, T.lib().tecto_last_error_string()) for r in res]
     for i, q in enumerate(reqs):
         ws = settings(q.plates, (40,))
         w = T.World(ws, q.width, q.height, seed=q.worldSeed)
@@ -105,3 +107,27 @@ def test_initialize_with_arguments(stream):
     np.testing.assert_array_equal(a.plates(stream), b.plates(stream))
     with pytest.raises(T.TectoError):
         T.check(T.lib().tecto_world_init(a.ptr, 0, gens, 2, stream.cuda_stream), "tecto_world_init")
+
+
+def test_batch_joins_worlds_initialised_differently(stream):
+    """Worlds whose settings differ only in initialisation fields share a batch; a world whose step
+    settings differ is refused."""
+    a = T.World(settings(6, (40,)), 64, 48, seed=1)
+    b = T.World(settings(9, (30, 70)), 64, 48, seed=2)
+    a.init_reference(stream)
+    b.init_reference(stream)
+    bt = T.Batch()
+    bt.add(a, stream)
+    bt.add(b, stream)
+    bt.step(2, stream)
+    stream.synchronize()
+    bt.check(stream)
+    c_settings = settings(6, (40,))
+    c_settings.kernel.gravity = 9.0
+    c = T.World(c_settings, 64, 48, seed=3)
+    c.init_reference(stream)
+    with pytest.raises(T.TectoError):
+        bt.add(c, stream)
+    bt.close()
+    for w in (a, b, c):
+        w.close()

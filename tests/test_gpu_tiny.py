@@ -33,10 +33,12 @@ def settings(kind):
     return s
 
 
+@pytest.mark.parametrize("tile", [0, 8])
 @pytest.mark.parametrize("kind", ["baseline", "reference"])
 @pytest.mark.parametrize("W,H", [(1, 1), (1, 7), (5, 1), (2, 3), (3, 2), (7, 5), (65, 3), (3, 70)])
-def test_tiny_worlds_match_oracle(stream, kind, W, H):
+def test_tiny_worlds_match_oracle(stream, kind, W, H, tile):
     s = settings(kind)
+    s.step.hydraulicTile = tile
     w = T.World(s, W, H, seed=500)
     w.init_synthetic(min(3, W * H), 1.7, 2, stream)
     if kind == "reference":

@@ -98,7 +98,7 @@ def test_world_autotune_keeps_results(stream):
     w.init_synthetic(12, 1.5, 5)
     h0 = w.download(T.FIELD_HEIGHT)
     t = w.autotune(stream)
-    assert 1 <= t.hydraulicTile <= 7 and 8 <= t.sortRadixBits <= 11
+    assert 1 <= t.hydraulicTile <= 8 and 8 <= t.sortRadixBits <= 11
     assert all(x > 0 for x in t.hydraulic_ms) and all(x > 0 for x in t.sort_ms)
     assert t.hydraulic_ms[t.hydraulicTile - 1] == min(t.hydraulic_ms)
     assert t.sort_ms[t.sortRadixBits - 8] == min(t.sort_ms)
@@ -127,7 +127,7 @@ def test_shape_autotune_and_batch_autotune(stream):
         b.add(w, stream)
         ws.append(w)
     tb = b.autotune(stream)
-    assert 1 <= tb.hydraulicTile <= 7 and 8 <= tb.sortRadixBits <= 11
+    assert 1 <= tb.hydraulicTile <= 8 and 8 <= tb.sortRadixBits <= 11
     b.step(2, stream)
     stream.synchronize()
     b.check(stream)
