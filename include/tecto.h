@@ -136,8 +136,10 @@ typedef struct tecto_step_settings {
     int hydraulicTile;        /* 0 = autotuner's choice, else 4; 1: 64x16/256 threads, 2: 64x32/256,
                                  3: 64x32/512, 4: 64x32/1024, 5: 64x64/1024, 6: 64x16/512 (3 blocks
                                  per SM), 7: 64x16/384 (4 blocks per SM), 8: column strips of 56
-                                 cells marched down by one warp each, no block barriers (the split
-                                 path, 50 dt >= 1.5, runs variant 4) */
+                                 cells marched down by one warp each, no block barriers, 9: column
+                                 strips of 120 cells marched down 8 rows at a time by a block of 512
+                                 threads, rows kept in shared memory (8 and 9: the split path,
+                                 50 dt >= 1.5, runs variant 4) */
     int thermalTile;          /* 0 = autotuner's choice, else 4; 1: 64x32 tiles / 1024 threads, up to 5
                                  iterations per launch; 2: 64x16 / 512, 2 blocks per SM, up to 4;
                                  3: 64x16 / 768, 2 blocks per SM, up to 3; 4: 64x16 / 512, 3 blocks
@@ -424,10 +426,10 @@ int tecto_batch_phase_thermal(tecto_batch *batch, int iterations, tecto_stream_t
  * the nearest tuned class on their device, else the defaults (hydraulic variant 4, thermal
  * variant 4, 8-bit digits). */
 typedef struct tecto_tuning {
-    int hydraulicTile;       /* chosen variant, 1..8 */
+    int hydraulicTile;       /* chosen variant, 1..9 */
     int sortRadixBits;       /* chosen digit width, 8..11 */
     int thermalTile;         /* chosen variant, 1..4 */
-    float hydraulic_ms[8];   /* one hydraulic sub-iteration with variant 1..8 */
+    float hydraulic_ms[9];   /* one hydraulic sub-iteration with variant 1..9 */
     float sort_ms[4];        /* the collision sort with 8..11-bit digits */
     float thermal_ms[4];     /* ten thermal iterations with variant 1..4 */
 } tecto_tuning;

@@ -39,11 +39,12 @@ void build_tiles(const Batch &b, int kind, std::vector<uint2> &out)
 void build_strips(const Batch &b, std::vector<uint4> &out, unsigned long long *rows)
 {
     out.clear();
+    const int inner = b.hydro_variant == kHydroMarchVariant ? kMarchInner : kStripInner;
     unsigned long long r = 0;
     for (size_t wi = 0; wi < b.members.size(); ++wi) {
         const tecto_world *w = b.members[wi];
-        for (int x0 = 0; x0 < w->W; x0 += kStripInner) {
-            const int iw = std::min(kStripInner, w->W - x0);
+        for (int x0 = 0; x0 < w->W; x0 += inner) {
+            const int iw = std::min(inner, w->W - x0);
             out.push_back(make_uint4((unsigned)wi, (unsigned)x0, (unsigned)iw, (unsigned)r));
             r += (unsigned long long)w->H;
         }

@@ -337,11 +337,14 @@ void gaussian_weights(float sigma, int radius, float *out);
 int ensure_kernel_attributes();
 int hydro_variant_for(const tecto_settings &s);  // 0 when the settings leave the choice open
 constexpr int kDefaultRadixBits = 8;
-constexpr int kHydroVariantCount = 8;
+constexpr int kHydroVariantCount = 9;
 constexpr int kDefaultHydroVariant = 4;          // 64 x 32 cells, 1024 threads
-constexpr int kHydroStripVariant = 8;            // marching column strips (fused path only)
-constexpr int kStripInner = 56;                  // interior columns of one strip (64 with the halo)
-// the strip table of a batch: every member's columns cut into strips of kStripInner
+constexpr int kHydroStripVariant = 8;            // marching column strips in registers (fused path only)
+constexpr int kHydroMarchVariant = 9;            // marching row chunks in shared memory (fused path only)
+constexpr int kStripInner = 56;                  // interior columns of one register strip (64 with the halo)
+constexpr int kMarchInner = 120;                 // interior columns of one shared-memory strip (128 with it)
+// the strip table of a batch: every member's columns cut into strips of kMarchInner columns for
+// kHydroMarchVariant, of kStripInner otherwise
 void build_strips(const Batch &b, std::vector<uint4> &out, unsigned long long *rows);
 constexpr int kThermalVariantCount = 4;
 constexpr int kDefaultThermalVariant = 4;        // 64 x 16 cells, 512 threads, 2 iterations per launch

@@ -39,7 +39,7 @@ def test_later_record_replaces():
     assert T.autotune_lookup(0, 1 << 22, 1) == (5, 10, 3)
 
 
-@pytest.mark.parametrize("args", [(0, 1 << 20, 1, 0, 8, 1), (0, 1 << 20, 1, 9, 8, 1), (0, 1 << 20, 1, 4, 7, 1),
+@pytest.mark.parametrize("args", [(0, 1 << 20, 1, 0, 8, 1), (0, 1 << 20, 1, 10, 8, 1), (0, 1 << 20, 1, 4, 7, 1),
                                   (0, 1 << 20, 1, 4, 12, 1), (0, 0, 1, 4, 8, 1), (0, 1 << 20, 0, 4, 8, 1),
                                   (-1, 1 << 20, 1, 4, 8, 1), (0, 1 << 20, 1, 4, 8, 0), (0, 1 << 20, 1, 4, 8, 5)])
 def test_invalid_records_rejected(args):

@@ -113,14 +113,16 @@ def test_phases_match_oracle(kind, W, H):
     print(kind, W, H, {k: max(v) for k, v in report.items()})
 
 
-@pytest.mark.parametrize("tile", [1, 2, 3, 4, 5, 6, 7, 8])
+@pytest.mark.parametrize("tile", [1, 2, 3, 4, 5, 6, 7, 8, 9])
 @pytest.mark.parametrize("W,H,dt", [(100, 60, 0.02), (33, 17, 0.02), (300, 200, 0.02), (128, 96, 1.0),
                                     (57, 130, 0.02), (112, 9, 0.02), (170, 257, 0.029)])
 def test_hydraulic_tile_variants_match_oracle(tile, W, H, dt):
     """Every hydraulic tile shape (interior tiles without wrap, edge tiles with it) gives the
     oracle's result; dt 1.0 takes the split transport path.  Variant 8 marches column strips of 56
     interior columns: 57 and 112 columns end on a strip of one column and on a whole strip, odd
-    widths take the unpaired loads, and dt 0.029 lets transport reach nearly 1.5 cells."""
+    widths take the unpaired loads, and dt 0.029 lets transport reach nearly 1.5 cells.  Variant 9
+    marches strips of 120 columns in chunks of 8 rows: 9 and 17 rows end inside the first or
+    third chunk, 300 columns end on a strip of 60, and 170 x 257 ends on both."""
     st, w = make_world("baseline", W, H)
     st.step.hydraulicTile = tile
     w.set_settings(st)

@@ -33,7 +33,7 @@ def settings(kind):
     return s
 
 
-@pytest.mark.parametrize("tile", [0, 8])
+@pytest.mark.parametrize("tile", [0, 8, 9])
 @pytest.mark.parametrize("kind", ["baseline", "reference"])
 @pytest.mark.parametrize("W,H", [(1, 1), (1, 7), (5, 1), (2, 3), (3, 2), (7, 5), (65, 3), (3, 70)])
 def test_tiny_worlds_match_oracle(stream, kind, W, H, tile):

@@ -98,7 +98,7 @@ def test_world_autotune_keeps_results(stream):
     w.init_synthetic(12, 1.5, 5)
     h0 = w.download(T.FIELD_HEIGHT)
     t = w.autotune(stream)
-    assert 1 <= t.hydraulicTile <= 8 and 8 <= t.sortRadixBits <= 11
+    assert 1 <= t.hydraulicTile <= 9 and 8 <= t.sortRadixBits <= 11
     assert all(x > 0 for x in t.hydraulic_ms) and all(x > 0 for x in t.sort_ms)
     assert t.hydraulic_ms[t.hydraulicTile - 1] == min(t.hydraulic_ms)
     assert t.sort_ms[t.sortRadixBits - 8] == min(t.sort_ms)
