@@ -253,10 +253,18 @@ def run_reference(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+# steps timed per reference-kernel case; the engine's plain_2048 / plain_8192 rows time as many
+REF_GPU_STEPS = {"2048": 20, "8192": 5}
+REF_GPU_OMITS = ("processCollisions is not launched (applyInelasticCollision reads past a local array; a "
+                 "height and id copy stands in for it), and neither is the reference uplift chain "
+                 "(moveContinentalCollisions, combinePropagatedCollisions, JFA*, applyUplift); the engine's "
+                 "step runs its resolve and uplift, so the speed-up is a lower bound")
+
+
 def reference_gpu_lines(s):
     """The reference's own CUDA kernels on this GPU (oracle/refgpu/ref_gpu_harness.cpp), one world
     at a time, at 2048^2 (32 plates) and 8192^2 (64 plates, velocities in [-2, 2], 8-connected CCL
-    every step)."""
+    every step), over REF_GPU_STEPS steps after 2 warm-up steps."""
     try:
         import torch
 
@@ -268,8 +276,8 @@ def reference_gpu_lines(s):
     out = {"kernels": "getPixelMovements, registerPlateCollisions, determineCollisionType, "
                       "createCollisionTypeMatrix, thermalErosionKernel x thermal iterations, rain/flux/flow/"
                       "sediment/transport/evaporate + 2 copies x hydraulic iterations, copies back, "
-                      "applyAccretion, CCL when due; processCollisions not launched (reads past a local "
-                      "array), a height copy stands in for it",
+                      "applyAccretion, CCL when due",
+           "omitted": REF_GPU_OMITS,
            "launch": "256 threads per block, one thread per cell, one stream, no per-launch synchronisation"}
     # the reference's kernels print diagnostics from the device; keep them off stdout, which
     # carries the JSON line
@@ -282,8 +290,9 @@ def reference_gpu_lines(s):
                 h, ids, pl = O.generate_world(W, W, P, vel, 1)
                 st = O.baseline_settings()
                 st.sim.iterationsForCCL = ccl_every
-                ms = O.ref_gpu_time(W, W, h, ids, pl, st, steps=5 if W <= 2048 else 3, warmup=2)
-                out[name] = {"value": W * W / (ms / 1e3), "unit": "cell-updates/s", "ms_per_step": ms}
+                ms = O.ref_gpu_time(W, W, h, ids, pl, st, steps=REF_GPU_STEPS[name], warmup=2)
+                out[name] = {"value": W * W / (ms / 1e3), "unit": "cell-updates/s", "ms_per_step": ms,
+                             "steps": REF_GPU_STEPS[name]}
             except Exception as e:  # noqa: BLE001
                 out[name] = {"unavailable": f"{type(e).__name__}: {e}"}
         torch.cuda.synchronize()
@@ -330,9 +339,53 @@ def reduce_max(x, dist, device):
     return float(t.item())
 
 
-def job_rate(ws, cells_per_rank, steps, ms_max):
-    """Whole-job cell-updates/s: every rank's cells times the steps, over the slowest rank's time."""
-    return ws * cells_per_rank * steps / (ms_max / 1e3)
+def reduce_sum(x, dist, device):
+    """x summed over the ranks (every replica's cells), or x alone without a process group."""
+    import torch
+
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+class EventClock:
+    """Device time on the launching stream: CUDA events recorded before and after the steps."""
+
+    def __init__(self, torch, stream):
+        self.stream = stream
+        self.e0 = torch.cuda.Event(enable_timing=True)
+        self.e1 = torch.cuda.Event(enable_timing=True)
+
+    def start(self):
+        self.e0.record(self.stream)
+
+    def stop(self):
+        self.e1.record(self.stream)
+
+    def ms(self):
+        return self.e0.elapsed_time(self.e1)
+
+
+def timed_region(step, steps, clock, sync, barrier, max_over_ranks):
+    """The timed region every rank runs on its own replica: a barrier and a synchronize, `steps`
+    steps between the clock's marks, a synchronize and a barrier.  Returns (this rank's ms, the
+    slowest rank's ms)."""
+    barrier()
+    sync()
+    clock.start()
+    step(steps)
+    clock.stop()
+    sync()
+    barrier()
+    mine = clock.ms()
+    return mine, max_over_ranks(mine)
+
+
+def job_rate(cells_all_ranks, steps, ms_max):
+    """Whole-job cell-updates/s: the cells of every rank's replica (summed over the ranks) times the
+    steps, over the slowest rank's time."""
+    return cells_all_ranks * steps / (ms_max / 1e3)
 
 
 def run_engine(args, ws, rank, local):
@@ -372,19 +425,13 @@ def run_engine(args, ws, rank, local):
     batch.check(stream)
 
     launches0 = batch.launches
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
-        barrier()
-        torch.cuda.synchronize()
-        e0.record(stream)
-        batch.step(args.steps, stream)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        barrier()
-    ms = max_over_ranks(e0.elapsed_time(e1))
+        _, ms = timed_region(lambda n: batch.step(n, stream), args.steps, EventClock(torch, stream),
+                             torch.cuda.synchronize, barrier, max_over_ranks)
     launches = batch.launches - launches0
     batch.check(stream)
-    value = job_rate(ws, total, args.steps, ms)
+    total_all = reduce_sum(total, dist, "cuda")  # replicas hold different worlds
+    value = job_rate(total_all, args.steps, ms)
 
     # dominant kernel: the fused hydraulic sub-iteration over the whole batch, on the same stream
     reps = 20
@@ -440,7 +487,7 @@ def run_engine(args, ws, rank, local):
     e2e_run(e2e_steps)
     wall_ms = (time.perf_counter() - t0) * 1e3
     e2e_ms = max_over_ranks(wall_ms)
-    e2e_value = job_rate(ws, total, e2e_steps, e2e_ms)
+    e2e_value = job_rate(total_all, e2e_steps, e2e_ms)
     h2d = sum(t.numel() * t.element_size() for hs in hosts for t in hs.values())
     d2h = sum(t.numel() * t.element_size() for os_ in outs for t in os_.values())
     batch.check(stream)
@@ -526,7 +573,7 @@ def engine_extras(args, T, torch, stream, s, specs, total, batched_value):
                     "batched_vs_plain": batched_value / plain_value}
 
     # plain one-world references
-    v2048, ms2048 = plain_world_rate(T, torch, stream, 2048, 2048, 32, 1.0, 20, s)
+    v2048, ms2048 = plain_world_rate(T, torch, stream, 2048, 2048, 32, 1.0, REF_GPU_STEPS["2048"], s)
     w = T.World(s, 2048, 2048, seed=1000)
     w.init_synthetic_device(32, 1.0, 1)
     w.step(1, stream)
@@ -541,11 +588,25 @@ def engine_extras(args, T, torch, stream, s, specs, total, batched_value):
     s2 = T.baseline_settings()
     s2.sim.iterationsForCCL = 1
     s2.step.cclConnectivity = T.CCL_8
-    v8192, ms8192 = plain_world_rate(T, torch, stream, 8192, 8192, 64, 2.0, 5, s2)
+    v8192, ms8192 = plain_world_rate(T, torch, stream, 8192, 8192, 64, 2.0, REF_GPU_STEPS["8192"], s2)
     out["plain_8192"] = {"value": v8192, "unit": "cell-updates/s", "ms_per_step": ms8192,
                          "workload": "one 8192x8192 world, 64 plates, velocities in [-2, 2], 8-connected CCL "
                                      "every step",
                          "step_roofline_frac": (STEP_BYTES_PER_CELL + 4.5) * v8192 / 1e9 / peak}
+    torch.cuda.empty_cache()
+
+    # the reference's own CUDA kernels on this GPU, the same worlds, as many steps as plain_2048 / 8192
+    ref = reference_gpu_lines(s)
+    vs = {"omitted_from_reference": REF_GPU_OMITS}
+    for name, v, ms in (("2048", v2048, ms2048), ("8192", v8192, ms8192)):
+        r = ref.get(name, {})
+        if "ms_per_step" in r:
+            vs[name] = {"engine_ms_per_step": ms, "reference_ms_per_step": r["ms_per_step"],
+                        "engine_value": v, "reference_value": r["value"], "unit": "cell-updates/s",
+                        "speedup": r["ms_per_step"] / ms, "steps": r["steps"]}
+        else:
+            vs[name] = r
+    out["vs_reference_gpu"] = vs
     torch.cuda.empty_cache()
 
     # the widened rows: plate dynamics' cost per step, the reference's initialisation, the exports

@@ -59,12 +59,79 @@ def test_two_gloo_ranks():
     assert ref1 is None                    # the reference arm: rank 0 alone
 
 
+class _WallClock:
+    def start(self):
+        import time
+        self.t0 = time.perf_counter()
+
+    def stop(self):
+        import time
+        self.t1 = time.perf_counter()
+
+    def ms(self):
+        return (self.t1 - self.t0) * 1e3
+
+
+def _replica_rank(rank, ws, port, out):
+    """run_engine's replica bookkeeping with the CPU oracle standing in for the engine: each rank
+    steps the two smallest worlds of its own batch inside bench.timed_region, the slowest rank's
+    time comes back on every rank, and the job rate counts every rank's cells."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+    import oracle as O
+
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(ws),
+                      LOCAL_RANK=str(rank))
+    dist.init_process_group("gloo", rank=rank, world_size=ws)
+    try:
+        s = O.baseline_settings()
+        specs = sorted(bench.rank_worlds(rank), key=lambda x: x[0] * x[1])[:2]
+        worlds = []
+        for W, H, P, gs, wsd in specs:
+            h, ids, pl = O.generate_world(W, H, P, 1.0, gs)
+            worlds.append(O.OracleWorld(s, h, ids, pl, wsd))
+        before = [w.h.copy() for w in worlds]
+
+        def step(n):
+            for w in worlds:
+                w.step(n)
+
+        mine, slowest = bench.timed_region(step, 2, _WallClock(), lambda: None, dist.barrier,
+                                           lambda x: bench.reduce_max(x, dist, "cpu"))
+        cells = sum(W * H for W, H, *_ in specs)
+        moved = all(not (w.h == b).all() for w, b in zip(worlds, before))
+        cells_all = bench.reduce_sum(cells, dist, "cpu")
+        out.put((rank, mine, slowest, cells, [sp[:2] for sp in specs], moved,
+                 bench.job_rate(cells_all, 2, slowest)))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_step_their_replicas():
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = free_port()
+    procs = [ctx.Process(target=_replica_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=300) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    (_, mine0, slow0, cells0, shapes0, moved0, rate0), (_, mine1, slow1, cells1, shapes1, moved1, rate1) = res
+    assert moved0 and moved1                         # both replicas stepped
+    assert shapes0 != shapes1                        # each rank its own worlds
+    assert slow0 == slow1 == max(mine0, mine1)       # the slowest rank's time on every rank
+    assert cells0 != cells1                          # replicas of different sizes
+    assert rate0 == rate1 == pytest.approx((cells0 + cells1) * 2 / (slow0 / 1e3))  # every rank's own cells
+
+
 def test_job_rate_aggregates_ranks():
     sys.path.insert(0, str(ROOT))
     import bench
 
-    assert bench.job_rate(1, 1000, 4, 2.0) == pytest.approx(2.0e6)
-    assert bench.job_rate(4, 1000, 4, 2.0) == pytest.approx(8.0e6)
+    assert bench.job_rate(1000, 4, 2.0) == pytest.approx(2.0e6)
+    assert bench.job_rate(1000 + 3000, 4, 2.0) == pytest.approx(8.0e6)
 
 
 def test_rooflines_from_the_committed_profiles():
