@@ -458,7 +458,10 @@ size_t tecto_world_bytes(int width, int height);
  * them one step per tick as one batch, admits waiting requests first-come first-served whenever
  * their tecto_world_bytes fit the budget (and fewer than max_worlds are active), and retires
  * finished worlds at once, so new requests join while others are mid-flight.  A request larger
- * than the whole budget is rejected (TECTO_ERR_BUDGET). */
+ * than the whole budget is rejected (TECTO_ERR_BUDGET).  Heavy requests (tecto_server_set_policy;
+ * by default worlds of 2^20 cells or more, which already run near the GPU's full rate alone) are
+ * live at most one at a time, first-come first-served among themselves; light requests join past
+ * a heavy one that waits for its slot, but never past one that waits for budget. */
 typedef struct tecto_server tecto_server;
 typedef struct tecto_request {
     int width, height, plates, steps;
@@ -513,6 +516,10 @@ int tecto_server_set_output(tecto_server *server, const char *directory, int wha
 int tecto_server_set_init(tecto_server *server, int mode);
 /* Dry-run cost model: seconds one tick takes per million active cells (default 2e-4). */
 int tecto_server_set_dry_cost(tecto_server *server, double seconds_per_mcell_step);
+/* Size-aware admission: requests of at least heavy_cells cells are heavy, and at most heavy_slots
+ * of them are live at a time (defaults 2^20 and 1).  heavy_slots = 0 lifts the limit: every
+ * request joins as soon as it fits.  Applies to trace replays and live serving alike. */
+int tecto_server_set_policy(tecto_server *server, size_t heavy_cells, int heavy_slots);
 
 /* ---- live serving: requests submitted as they come, the caller drives the ticks ----------
  *

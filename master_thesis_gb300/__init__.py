@@ -294,6 +294,7 @@ def _declare(L: C.CDLL) -> None:
         "tecto_server_run_trace_sequential": ([P, C.POINTER(Request), C.c_int, P, C.POINTER(RequestResult),
                                                C.POINTER(ServerStats)], C.c_int),
         "tecto_server_set_dry_cost": ([P, C.c_double], C.c_int),
+        "tecto_server_set_policy": ([P, C.c_size_t, C.c_int], C.c_int),
         "tecto_server_set_init": ([P, C.c_int], C.c_int),
         "tecto_server_set_output": ([P, C.c_char_p, C.c_int, C.c_float, C.c_float], C.c_int),
         "tecto_server_submit": ([P, C.POINTER(Request), C.POINTER(C.c_int)], C.c_int),
@@ -719,6 +720,10 @@ class Server:
 
     def set_dry_cost(self, seconds_per_mcell_step: float) -> None:
         check(lib().tecto_server_set_dry_cost(self.ptr, seconds_per_mcell_step), "tecto_server_set_dry_cost")
+
+    def set_policy(self, heavy_cells: int, heavy_slots: int) -> None:
+        """Requests of at least heavy_cells cells are live at most heavy_slots at a time (0: no limit)."""
+        check(lib().tecto_server_set_policy(self.ptr, heavy_cells, heavy_slots), "tecto_server_set_policy")
 
     def _run(self, fn, requests, stream):
         n = len(requests)

@@ -6,6 +6,12 @@
 // first-come first-served whenever their footprint fits the HBM budget; finished worlds leave the
 // batch at once so that newcomers join while others are mid-flight.  World state stays resident
 // in HBM from admission to completion.
+//
+// Size-aware admission: a world of at least `heavy_cells` cells (2^20 by default) already runs near
+// the GPU's full rate on its own, so sharing ticks with another such world only slows both, while
+// smaller worlds gain from riding along in a batch.  At most `heavy_slots` (1) heavy requests are
+// live at a time, admitted first-come first-served among themselves; light requests are admitted
+// past a heavy one that waits for its slot (never past one that waits for budget).
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -63,6 +69,8 @@ struct tecto_server {
     int max_worlds = 0;
     bool dry = false;
     double dry_cost = 2e-4;  // seconds per tick per million active cells
+    size_t heavy_cells = (size_t)1 << 20;  // tecto_server_set_policy
+    int heavy_slots = 1;                    // 0: no limit (every request joins once it fits)
     tecto_batch *batch = nullptr;
     std::string out_dir;     // where finished requests are written (tecto_server_set_output)
     int out_what = 0;        // TECTO_SERVER_OUT_* bits
@@ -179,34 +187,49 @@ bool valid_request(const tecto_request &r)
            (size_t)r.width * (size_t)r.height <= ((size_t)1 << 30);
 }
 
-// Drops the head of the queue if it can never be served (invalid, or larger than the whole budget);
-// returns whether it did.
-bool reject_head(const tecto_server *sv, Serving &q, const tecto_request *req, tecto_request_result *res)
+// Whether a waiting request can never be served (invalid, or larger than the whole budget): its
+// status is set and it leaves the queue.
+bool reject(const tecto_server *sv, Serving &q, std::deque<int>::iterator &it, const tecto_request *req,
+            tecto_request_result *res)
 {
-    const int i = q.waiting.front();
+    const int i = *it;
     const tecto_request &r = req[i];
     int status = TECTO_OK;
     if (!valid_request(r)) status = TECTO_ERR_INVALID;
     else if (world_footprint(r.width, r.height) > sv->budget) status = TECTO_ERR_BUDGET;
     if (status == TECTO_OK) return false;
     res[i].status = status;
-    q.waiting.pop_front();
+    it = q.waiting.erase(it);
     ++q.done;
     return true;
 }
 
-// Admission: waiting requests join first come first served while their footprint fits the budget
-// and fewer than max_worlds are active; the first that does not fit stops admission (no overtaking).
+bool heavy(const tecto_server *sv, size_t cells) { return sv->heavy_slots > 0 && cells >= sv->heavy_cells; }
+
+// Admission, in arrival order: a request joins while its footprint fits the budget and fewer than
+// max_worlds are active, and the first that does not fit stops admission (no overtaking past it).
+// A heavy request also needs a free heavy slot and no earlier heavy request waiting; while it waits
+// for that, later light requests may join.
 void admit(tecto_server *sv, Serving &q, const tecto_request *req, tecto_request_result *res, cudaStream_t st,
           const ServeClock &c)
 {
-    while (!q.waiting.empty()) {
-        if (reject_head(sv, q, req, res)) continue;
-        const int i = q.waiting.front();
+    int heavy_live = 0;
+    for (const Live &L : q.live) heavy_live += heavy(sv, L.cells) ? 1 : 0;
+    bool heavy_waits = false;  // an earlier heavy request waits for its slot
+    for (auto it = q.waiting.begin(); it != q.waiting.end();) {
+        if (reject(sv, q, it, req, res)) continue;
+        const int i = *it;
         const tecto_request &r = req[i];
+        const size_t cells = (size_t)r.width * (size_t)r.height;
+        const bool hv = heavy(sv, cells);
+        if (hv && (heavy_waits || heavy_live >= sv->heavy_slots)) {
+            heavy_waits = true;
+            ++it;
+            continue;
+        }
         const size_t bytes = world_footprint(r.width, r.height);
         if (q.used + bytes > sv->budget || (int)q.live.size() >= sv->max_worlds) break;
-        Live L{i, nullptr, bytes, (size_t)r.width * (size_t)r.height, r.steps};
+        Live L{i, nullptr, bytes, cells, r.steps};
         if (!sv->dry) {
             // a world that cannot be created (out of memory, say) fails its own request only
             int rc = make_world(sv, r, st, &L.world);
@@ -214,7 +237,7 @@ void admit(tecto_server *sv, Serving &q, const tecto_request *req, tecto_request
                 tecto_world_destroy(L.world);
             if (rc != TECTO_OK) {
                 res[i].status = rc;
-                q.waiting.pop_front();
+                it = q.waiting.erase(it);
                 ++q.done;
                 continue;
             }
@@ -223,8 +246,9 @@ void admit(tecto_server *sv, Serving &q, const tecto_request *req, tecto_request
         q.peak = std::max(q.peak, (double)q.used);
         res[i].admit_s = c.now();
         q.live.push_back(L);
-        q.waiting.pop_front();
+        it = q.waiting.erase(it);
         q.changed = true;
+        heavy_live += hv ? 1 : 0;
     }
 }
 
@@ -353,6 +377,17 @@ int tecto_server_set_dry_cost(tecto_server *sv, double s)
 {
     if (!sv || !(s >= 0)) return TECTO_ERR_INVALID;
     sv->dry_cost = s;
+    return TECTO_OK;
+}
+
+int tecto_server_set_policy(tecto_server *sv, size_t heavy_cells, int heavy_slots)
+{
+    if (!sv || heavy_slots < 0 || (heavy_slots > 0 && heavy_cells == 0)) {
+        set_error("tecto_server_set_policy: invalid argument");
+        return TECTO_ERR_INVALID;
+    }
+    sv->heavy_cells = heavy_cells;
+    sv->heavy_slots = heavy_slots;
     return TECTO_OK;
 }
 

@@ -92,3 +92,42 @@ def test_output_settings_are_checked_and_dry_runs_write_nothing(tmp_path):
     assert st.completed == 2 and all(r.status == 0 for r in res)
     assert list(tmp_path.iterdir()) == []
     sv.set_output(None, 0)  # off again
+
+
+def test_heavy_requests_run_one_at_a_time_and_light_ones_ride_along():
+    # two heavy requests (2^20 cells each) and a light one arriving while the second heavy waits:
+    # the heavies run one after the other in arrival order, the light one joins at once
+    reqs = [req(1024, 1024, 20, 0.0, seed=1), req(2048, 512, 20, 0.001, seed=2), req(256, 256, 5, 0.002, seed=3)]
+    sv = T.Server(T.baseline_settings(), 10 * T.world_bytes(2048, 512), dry_run=True)
+    sv.set_dry_cost(1e-3)
+    res, st = sv.run_trace(reqs)
+    assert st.completed == 3
+    assert res[1].admit_s >= res[0].finish_s                   # one heavy at a time
+    assert res[2].admit_s < res[0].finish_s                    # the light one overtakes the waiting heavy
+    assert res[2].finish_s < res[1].admit_s
+    # with the limit lifted both heavies overlap again
+    sv.set_policy(1 << 20, 0)
+    res2, st2 = sv.run_trace(reqs)
+    assert st2.completed == 3 and res2[1].admit_s < res2[0].finish_s
+    # two heavy slots: both heavies overlap, a third waits for a slot in arrival order
+    sv.set_policy(1 << 20, 2)
+    reqs3 = reqs[:2] + [req(1024, 1024, 20, 0.0015, seed=4)] + reqs[2:]
+    res3, st3 = sv.run_trace(reqs3)
+    assert st3.completed == 4
+    assert res3[1].admit_s < res3[0].finish_s
+    assert res3[2].admit_s >= min(res3[0].finish_s, res3[1].finish_s)
+    # a lower threshold makes the 256^2 request heavy too: it waits for the first heavy
+    sv.set_policy(256 * 256, 1)
+    res4, _ = sv.run_trace(reqs)
+    assert res4[2].admit_s >= res4[1].finish_s
+
+
+def test_policy_arguments_are_checked():
+    sv = T.Server(T.baseline_settings(), T.world_bytes(256, 256), dry_run=True)
+    for bad in ((1 << 20, -1), (0, 1)):
+        try:
+            sv.set_policy(*bad)
+        except T.TectoError:
+            continue
+        raise AssertionError(f"accepted {bad}")
+    sv.set_policy(0, 0)
