@@ -706,6 +706,11 @@ def engine_extras(args, T, torch, stream, s, specs, total, batched_value):
 def run_case(args):
     """Small fixed workloads for ncu captures (no timing, no JSON line):
     erosion2048  one 5-iteration thermal launch and one fused hydraulic launch on a 2048^2 world;
+    erosion4096  the same on a 4096^2 world (each field 67 MB: a launch's working set is about
+                 eight times the L2), one thermal launch of the default variant, two hydraulic
+                 sub-iterations of the variant --hydro-tile (default 4);
+    collide4096  three collide phases of one 4096^2 world (16 777 216 keys: the sort passes in their
+                 form for large sorts), 8-bit sort digits;
     plain2048    4 steps of one 2048^2 world, 32 plates;
     policy2048   the same with plate dynamics, relabel after a CCL on every step, and merges;
     collide2048  three collide phases (advection fused into the sort, winner pick, collision types)
@@ -725,6 +730,21 @@ def run_case(args):
         w.upload(T.FIELD_SEDIMENT, np.abs(rng.normal(0, 0.01, (2048, 2048))).astype(np.float32))
         w.thermal(5, stream)
         w.hydraulic(1, s.step.hydraulicDt, stream)
+        w.check(stream)
+    elif args.case == "erosion4096":
+        s.step.hydraulicTile = args.hydro_tile
+        w = T.World(s, 4096, 4096, seed=1000)
+        w.init_synthetic_device(32, 1.0, 1)
+        w.step(1, stream)
+        w.thermal(2, stream)
+        w.hydraulic(2, s.step.hydraulicDt, stream)
+        w.check(stream)
+    elif args.case == "collide4096":
+        s.step.sortRadixBits = 8
+        w = T.World(s, 4096, 4096, seed=1000)
+        w.init_synthetic_device(32, 1.0, 1)
+        for _ in range(3):
+            w.collide(stream)
         w.check(stream)
     elif args.case == "policy2048":
         s.step.plateDynamics = T.PLATE_DYNAMICS_REFERENCE
@@ -747,7 +767,7 @@ def run_case(args):
         w.step(4, stream)
         w.check(stream)
     else:
-        s.step.hydraulicTile = 4
+        s.step.hydraulicTile = args.hydro_tile
         s.step.sortRadixBits = 9
         b = T.Batch()
         worlds = []
@@ -770,7 +790,9 @@ def main():
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
     ap.add_argument("--serve-requests", type=int, default=64)
     ap.add_argument("--quick", action="store_true", help="headline only (no plain/served/large-world lines)")
-    ap.add_argument("--case", choices=["erosion2048", "plain2048", "policy2048", "collide2048", "batch"],
+    ap.add_argument("--hydro-tile", type=int, default=4, help="hydraulic variant of the --case captures")
+    ap.add_argument("--case", choices=["erosion2048", "erosion4096", "plain2048", "policy2048", "collide2048",
+                                       "collide4096", "batch"],
                     help="a small fixed workload for profilers")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)

@@ -140,6 +140,31 @@ def ref_gpu_time(W, H, h, ids, plates, settings, steps=5, warmup=2):
     return ms.value
 
 
+def ref_gpu_relabel(ids, plate_sizes, settings, max_rounds=16):
+    """The reference's own CCL relabel (refgpu/ref_relabel.cu: its CCL, createPlateIdLabelMap, the
+    thrust ranking, getMaxSizeLabels, createLabelIdLookup, postCClIdReassign and the
+    assignUnassignedIdsToNeighbor passes) on this GPU.  Returns (ids, labels, markers, rounds,
+    unassigned): markers[k] is the plate whose record slot k holds afterwards."""
+    if not REF_CUBIN.exists():
+        raise RuntimeError("the reference's device code was not built (oracle/_ref/ref_kernels.cubin is absent)")
+    L = C.CDLL(str(REF_GPU_LIB))
+    L.refgpu_relabel_error.restype = C.c_char_p
+    L.refgpu_relabel.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                 C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    out = np.ascontiguousarray(ids, np.uint8).copy()
+    H, W = out.shape
+    sizes = np.ascontiguousarray(plate_sizes, np.int32)
+    assert sizes.shape == (255,)
+    labels = np.zeros((H, W), np.uint32)
+    markers = np.zeros(255, np.float32)
+    rounds, left = C.c_int(), C.c_int()
+    rc = L.refgpu_relabel(str(REF_CUBIN).encode(), W, H, _P(out), _P(sizes), C.addressof(settings.kernel),
+                          _P(labels), _P(markers), max_rounds, C.byref(rounds), C.byref(left))
+    if rc != 0:
+        raise RuntimeError(L.refgpu_relabel_error().decode())
+    return out, labels, markers, rounds.value, left.value
+
+
 REF_EXPORT_CUBIN = HERE / "_ref" / "ref_export.cubin"
 
 

@@ -1,8 +1,10 @@
 """Plate relabel and merges in the oracle.  Merges are pinned to the reference's own kernels
 (getNeighboringPlates, getPlateMerges run in thread order, clearCollisionTypes, the remap of
 mergeAndCountSizeMass; golden vectors).  The relabel's ranking and id assignment run in the
-reference inside one block with a barrier and atomics, which the CPU build cannot execute, so they
-are checked here case by case against createLabelIdLookup's rules."""
+reference inside one block with a barrier and atomics, which the CPU build cannot execute: they
+are pinned to the reference's own kernels run on a GPU (tests/golden/gen_golden_relabel.py, on id
+maps whose outcome does not depend on scheduling), and checked case by case against
+createLabelIdLookup's rules."""
 from __future__ import annotations
 
 import numpy as np
@@ -106,3 +108,25 @@ def test_policy_steps():
     w.step(6)
     assert (w.id != 255).all()
     assert len(np.unique(w.id)) <= n0 + 20
+
+
+@pytest.mark.parametrize("case", ["free_id", "no_free_id"])
+def test_relabel_matches_reference_kernels(golden, case):
+    """The oracle's relabel equals the reference's own applyCCL relabel (its CCL, thrust ranking,
+    getMaxSizeLabels, createLabelIdLookup, postCClIdReassign and assignUnassignedIdsToNeighbor, run
+    on a GPU): labels, final ids, and which plate record each id slot holds afterwards."""
+    g = golden("ref_relabel")
+    ids = g[f"{case}_ids_in"]
+    np.testing.assert_array_equal(labels_of(ids, T.CCL_REF8), g[f"{case}_labels"])
+    pl = np.zeros(255, T.PLATE_DTYPE)
+    dy = np.zeros(255, T.PLATE_DYNAMICS_DTYPE)
+    pl["velocity"] = np.arange(255)          # a record's marker: the plate it belonged to
+    dy["size"] = g[f"{case}_sizes"]
+    out, pl2, _, left = O.relabel(ids, g[f"{case}_labels"], pl, dy, int(g[f"{case}_min_plate_size"]))
+    assert left == 0
+    np.testing.assert_array_equal(out, g[f"{case}_ids_out"])
+    np.testing.assert_array_equal(pl2["velocity"], g[f"{case}_markers"])
+    # the cells postCClIdReassign left without an id: changed cells not moved to a new id's slot
+    moved = [k for k in range(255) if int(pl2["velocity"][k]) != k]
+    lost = int(((out != ids) & ~np.isin(out, moved)).sum())
+    assert lost == int(g[f"{case}_unassigned"]) > 0
