@@ -705,7 +705,8 @@ def engine_extras(args, T, torch, stream, s, specs, total, batched_value):
 
 def run_case(args):
     """Small fixed workloads for ncu captures (no timing, no JSON line):
-    erosion2048  one 5-iteration thermal launch and one fused hydraulic launch on a 2048^2 world;
+    erosion2048  one 5-iteration thermal launch and one fused hydraulic launch (variant --hydro-tile,
+                 default 4) on a 2048^2 world;
     erosion4096  the same on a 4096^2 world (each field 67 MB: a launch's working set is about
                  eight times the L2), one thermal launch of the default variant, two hydraulic
                  sub-iterations of the variant --hydro-tile (default 4);
@@ -723,6 +724,7 @@ def run_case(args):
     stream = torch.cuda.Stream()
     s = T.baseline_settings()
     if args.case == "erosion2048":
+        s.step.hydraulicTile = args.hydro_tile
         w = T.World(s, 2048, 2048, seed=1000)
         w.init_synthetic_device(32, 1.0, 1)
         rng = np.random.default_rng(1)
