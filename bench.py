@@ -66,36 +66,46 @@ def measured_peak_hbm():
     return 6800.0, "fallback 6.8 TB/s"
 
 
-def profiled_traffic_per_cell():
-    """dram bytes per cell of one k_hydro launch, from the committed ncu summary (2048^2 capture)."""
-    p = ROOT / "profiles" / "k_hydro_2048.md"
+MARCH_VARIANT = 9  # hydraulic variant of k_hydro_march
+
+
+def _profile_number(name, key):
+    p = ROOT / "profiles" / name
     if not p.exists():
         return None
-    m = re.search(r"traffic_bytes_per_launch_2048:\s*([0-9.eE+]+)", p.read_text())
-    return float(m.group(1)) / (2048 * 2048) if m else None
+    m = re.search(key + r":\s*([0-9.eE+]+)", p.read_text())
+    return float(m.group(1)) if m else None
 
 
-def profiled_instructions_per_cell():
-    """Warp-instructions per cell of one k_hydro launch, from the committed ncu summary (2048^2)."""
-    p = ROOT / "profiles" / "k_hydro_2048.md"
-    if not p.exists():
-        return None
-    m = re.search(r"warp_instructions_per_launch_2048:\s*([0-9.eE+]+)", p.read_text())
-    return float(m.group(1)) / (2048 * 2048) if m else None
+def profiled_traffic_per_cell(variant=MARCH_VARIANT):
+    """DRAM bytes per cell of one hydraulic launch from the committed ncu summaries: for the
+    marching kernel, captured on the mixed batch itself; for the tile kernels, a 2048^2 launch."""
+    if variant == MARCH_VARIANT:
+        return _profile_number("k_hydro_march_traffic.md", "traffic_bytes_per_cell_batch")
+    v = _profile_number("k_hydro_2048.md", "traffic_bytes_per_launch_2048")
+    return None if v is None else v / (2048 * 2048)
 
 
-def issue_roofline(ipc, cells, ms, sm_mhz, sms):
-    """k_hydro against the issue limit: every SM issues at most one warp-instruction per cycle on
-    each of its four schedulers."""
+def profiled_instructions_per_cell(variant=MARCH_VARIANT):
+    """Warp-instructions per cell of one hydraulic launch at 2048^2, from the committed ncu summary
+    of the kernel that variant runs."""
+    name = "k_hydro_march_2048.md" if variant == MARCH_VARIANT else "k_hydro_2048.md"
+    v = _profile_number(name, "warp_instructions_per_launch_2048")
+    return None if v is None else v / (2048 * 2048)
+
+
+def issue_roofline(ipc, cells, ms, sm_mhz, sms, kernel="k_hydro"):
+    """The hydraulic kernel against the issue limit: every SM issues at most one warp-instruction
+    per cycle on each of its four schedulers."""
     if ipc is None or not sm_mhz or not sms:
         return None
     achieved = ipc * cells / (ms / 1e3) / 1e9
     peak = sms * 4 * sm_mhz * 1e6 / 1e9
-    return {"bound": "issue", "kernel": "k_hydro", "achieved": achieved, "peak": peak,
+    return {"bound": "issue", "kernel": kernel, "achieved": achieved, "peak": peak,
             "unit": "G warp-instructions/s", "frac": achieved / peak,
-            "note": "warp-instructions per cell from one ncu capture of a 2048^2 launch (edge tiles of "
-                    "small worlds issue more, so the batch figure is a lower bound); peak = SMs x 4 "
-                    "schedulers x the SM clock sampled during the timed region"}
+            "note": "warp-instructions per cell from one ncu capture of a 2048^2 launch (narrow strips, "
+                    "edge tiles and short worlds issue more, so the batch figure is a lower bound); "
+                    "peak = SMs x 4 schedulers x the SM clock sampled during the timed region"}
 
 
 class ClockSampler:
@@ -439,8 +449,10 @@ def run_engine(args, ws, rank, local):
     hydro_ms = event_ms(torch, stream, lambda: batch.hydraulic(reps, s.step.hydraulicDt, stream)) / reps
     peak, peak_src = measured_peak_hbm()
     achieved = HYDRO_BYTES_PER_CELL * total / (hydro_ms / 1e3) / 1e9
-    tpc = profiled_traffic_per_cell()
-    ipc = profiled_instructions_per_cell()
+    hv = tuning.hydraulicTile
+    tpc = profiled_traffic_per_cell(hv)
+    ipc = profiled_instructions_per_cell(hv)
+    hkernel = "k_hydro_march" if hv == MARCH_VARIANT else "k_hydro"
     n_sms = torch.cuda.get_device_properties(local).multi_processor_count
 
     # e2e through the C ABI with host buffers: upload every world's state, step, download
@@ -520,13 +532,16 @@ def run_engine(args, ws, rank, local):
             "gpu_launches": int(launches),
             "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
-            "roofline": {"bound": "hbm", "kernel": "k_hydro (fused hydraulic sub-iteration, all worlds)",
+            "roofline": {"bound": "hbm", "kernel": f"{hkernel} (hydraulic variant {hv}: one fused sub-iteration, "
+                                                  "all worlds)",
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": None if tpc is None else tpc * total,
-                         "traffic_note": "ncu dram bytes of a 2048^2 launch, scaled per cell",
+                         "traffic_note": ("ncu dram bytes of one launch over this batch (profiles/k_hydro_march_traffic.md)"
+                                          if hv == MARCH_VARIANT else
+                                          "ncu dram bytes of a 2048^2 launch, scaled per cell"),
                          "peak_source": peak_src, "ms_per_launch": hydro_ms,
                          "alg_bytes_per_launch": HYDRO_BYTES_PER_CELL * total},
-            "issue_roofline": issue_roofline(ipc, total, hydro_ms, clk.summary().get("sm_mhz"), n_sms),
+            "issue_roofline": issue_roofline(ipc, total, hydro_ms, clk.summary().get("sm_mhz"), n_sms, hkernel),
             "step_roofline": {"alg_bytes_per_cell": STEP_BYTES_PER_CELL,
                               "achieved_gbs": STEP_BYTES_PER_CELL * value / ws / 1e9,
                               "frac": STEP_BYTES_PER_CELL * value / ws / 1e9 / peak},

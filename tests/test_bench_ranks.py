@@ -136,12 +136,16 @@ def test_job_rate_aggregates_ranks():
 
 def test_rooflines_from_the_committed_profiles():
     """The per-cell DRAM traffic and warp-instruction counts bench.py reports come from the committed
-    ncu summary of a 2048^2 k_hydro launch; the issue roofline is achieved / (SMs x 4 x clock)."""
+    ncu summaries (the marching kernel's traffic captured on the batch, the tile kernel's on a 2048^2
+    launch); the issue roofline is achieved / (SMs x 4 x clock)."""
     sys.path.insert(0, str(ROOT))
     import bench
 
-    tpc, ipc = bench.profiled_traffic_per_cell(), bench.profiled_instructions_per_cell()
-    assert tpc is not None and 40 < tpc < 80          # about 50 B/cell against 56 algorithmic
+    for v in (bench.MARCH_VARIANT, 4):
+        tpc, ipc = bench.profiled_traffic_per_cell(v), bench.profiled_instructions_per_cell(v)
+        assert tpc is not None and 40 < tpc < 80      # about 50-71 B/cell against 56 algorithmic
+        assert ipc is not None and 5 < ipc < 40       # warp-instructions per cell
+    tpc, ipc = bench.profiled_traffic_per_cell(4), bench.profiled_instructions_per_cell(4)
     assert ipc is not None and 5 < ipc < 40           # warp-instructions per cell
     r = bench.issue_roofline(ipc, 2048 * 2048, 0.1, 2070.0, 152)
     assert r["bound"] == "issue" and abs(r["peak"] - 152 * 4 * 2.07) < 1e-9
