@@ -30,25 +30,6 @@
 #include <string.h>
 #endif
 
-/* The sine series on a reduced argument r (|r| <= pi/4): r + r^3 (S3 + r^2 (S5 + ...)), each step
- * a fused multiply-add.  tecto_sincos_core evaluates its sine through this, and so may a caller
- * that knows the reduction is the identity (0 <= x < 0.78: rint(x 2/pi) = 0, and each reduction
- * step then subtracts an exact zero), with the same bits. */
-TECTO_HD float tecto_sin_series(float r)
-{
-    const float S3 = -1.6666666666666666e-1f;
-    const float S5 = 8.3333333333333332e-3f;
-    const float S7 = -1.9841269841269841e-4f;
-    const float S9 = 2.7557319223985893e-6f;
-    const float S11 = -2.5052108385441720e-8f;
-    const float r2 = r * r;
-    float ps = fmaf(r2, S11, S9);
-    ps = fmaf(r2, ps, S7);
-    ps = fmaf(r2, ps, S5);
-    ps = fmaf(r2, ps, S3);
-    return fmaf(r * r2, ps, r);
-}
-
 /* The shared core of tecto_sinf and tecto_cosf: the quadrant q of x and the sine and cosine of the
  * reduced argument.  Every step is a fused multiply-add (one rounding), the same on the GPU (FFMA)
  * and on the host (C99 fmaf, correctly rounded), so both sides still agree bit for bit; the
@@ -61,7 +42,12 @@ TECTO_HD void tecto_sincos_core(float x, int *q, float *s, float *c)
     const float C3 = 1.2665987014770508e-6f;
     const float C4 = 9.92093629470503e-10f;
     const float TWO_OVER_PI = 0.6366197466850281f;
-    /* Taylor coefficients 1/n! with alternating signs (the sine's in tecto_sin_series) */
+    /* Taylor coefficients 1/n! with alternating signs */
+    const float S3 = -1.6666666666666666e-1f;
+    const float S5 = 8.3333333333333332e-3f;
+    const float S7 = -1.9841269841269841e-4f;
+    const float S9 = 2.7557319223985893e-6f;
+    const float S11 = -2.5052108385441720e-8f;
     const float K2 = -0.5f;
     const float K4 = 4.1666666666666664e-2f;
     const float K6 = -1.3888888888888889e-3f;
@@ -74,7 +60,11 @@ TECTO_HD void tecto_sincos_core(float x, int *q, float *s, float *c)
     r = fmaf(-kf, C3, r);
     r = fmaf(-kf, C4, r);
     const float r2 = r * r;
-    *s = tecto_sin_series(r);
+    float ps = fmaf(r2, S11, S9);
+    ps = fmaf(r2, ps, S7);
+    ps = fmaf(r2, ps, S5);
+    ps = fmaf(r2, ps, S3);
+    *s = fmaf(r * r2, ps, r);
     float pc = fmaf(r2, K10, K8);
     pc = fmaf(r2, pc, K6);
     pc = fmaf(r2, pc, K4);

@@ -251,8 +251,6 @@ def lib() -> C.CDLL:
         L.or_lerp.restype = C.c_float
         L.or_sinf.argtypes = [C.c_float]
         L.or_sinf.restype = C.c_float
-        L.or_sin_series_mismatches.argtypes = [C.c_float, C.c_float, C.c_uint]
-        L.or_sin_series_mismatches.restype = C.c_ulong
         L.or_gaussian_weights.argtypes = [C.c_float, C.c_int, V]
         L.or_settings_default.argtypes = [V]
         L.or_settings_baseline.argtypes = [V]

@@ -161,24 +161,6 @@ float or_lerp(float a, float b, float t)
 static int g_libm_sin = 0;
 void or_use_libm_sin(int on) { g_libm_sin = on; }
 float or_sinf(float x) { return g_libm_sin ? sinf(x) : tecto_sinf(x); }
-
-/* Floats in [lo, hi) at every stride-th bit pattern where the engine's sine series alone (the
- * hydraulic kernels' shortcut when the reduction is the identity) differs from tecto_sinf. */
-unsigned long or_sin_series_mismatches(float lo, float hi, unsigned stride)
-{
-    unsigned a, b;
-    memcpy(&a, &lo, 4);
-    memcpy(&b, &hi, 4);
-    unsigned long bad = 0;
-    for (unsigned u = a; u < b; u += stride) {
-        float x, s1, s2;
-        memcpy(&x, &u, 4);
-        s1 = tecto_sinf(x);
-        s2 = tecto_sin_series(x);
-        if (memcmp(&s1, &s2, 4) != 0) ++bad;
-    }
-    return bad;
-}
 float or_expf(float x) { return tecto_expf(x); }
 float or_log10f(float x) { return tecto_log10f(x); }
 

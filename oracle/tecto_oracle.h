@@ -128,7 +128,6 @@ float or_rain_noise(int x, int y, int seed);
 float or_lerp(float a, float b, float t);
 void or_gaussian_weights(float sigma, int radius, float *w_out);
 float or_sinf(float x);
-unsigned long or_sin_series_mismatches(float lo, float hi, unsigned stride);
 void or_use_libm_sin(int on);
 
 /* The reference's default parameters and the benchmark's mapping of them (the same values as

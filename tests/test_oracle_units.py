@@ -105,12 +105,3 @@ def test_oracle_generator_equals_the_engines(W, H, P, vel, seed):
     np.testing.assert_array_equal(ho, he)
     np.testing.assert_array_equal(io, ie)
     np.testing.assert_array_equal(po.view(np.uint8), pe.view(np.uint8))
-
-
-def test_sine_series_alone_equals_the_full_sine_below_0_78():
-    """The hydraulic kernels evaluate the slope's sine by its series alone when every lane's argument
-    lies in [0.03, 0.78) (the reduction is then the identity): the same bits as tecto_sinf there,
-    checked on every float of the range."""
-    assert O.lib().or_sin_series_mismatches(0.03, 0.78, 1) == 0
-    # and above it the shortcut would be wrong, which is why the kernels test the range first
-    assert O.lib().or_sin_series_mismatches(0.8, 3.0, 97) > 0
