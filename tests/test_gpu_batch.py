@@ -25,11 +25,12 @@ def stream():
     return torch.cuda.Stream()
 
 
-def settings():
+def settings(tile=0):
     s = T.baseline_settings()
     s.kernel.minCollisionSize = 3
     s.kernel.collisionTypeUpdateCooldown = 2
     s.sim.iterationsForCCL = 3
+    s.step.hydraulicTile = tile
     return s
 
 
@@ -47,8 +48,11 @@ def assert_same(a: T.World, b: T.World, msg):
     assert a.iteration == b.iteration
 
 
-def test_batch_equals_alone_with_joins_and_leaves(stream):
-    s = settings()
+@pytest.mark.parametrize("tile", [4, 9])
+def test_batch_equals_alone_with_joins_and_leaves(stream, tile):
+    """Tiles (variant 4) and the marching kernel (variant 9), whose strip table and persistent
+    block ranges are rebuilt at every membership change."""
+    s = settings(tile)
     alone = [make(sp, s) for sp in SPECS]
     mixed = [make(sp, s) for sp in SPECS]
     # a world stepped alone first joins the batch with other ping-pong halves than the batch's

@@ -94,19 +94,22 @@ FIELDS = (T.FIELD_HEIGHT, T.FIELD_WATER, T.FIELD_SEDIMENT, T.FIELD_FLUX, T.FIELD
           T.FIELD_COLLISION, T.FIELD_TYPE_BITMAP)
 
 
-def batch_settings(rb):
+def batch_settings(rb, tile=4):
     s = T.baseline_settings()
     s.kernel.minCollisionSize = 3
     s.kernel.collisionTypeUpdateCooldown = 2
     s.sim.iterationsForCCL = 1
     s.step.sortRadixBits = rb
+    s.step.hydraulicTile = tile
     return s
 
 
-@pytest.mark.parametrize("rb", [8, 11])
-def test_batch_above_the_form_boundary_equals_worlds_alone(torch, rb):
+@pytest.mark.parametrize("rb,tile", [(8, 9), (11, 4)])
+def test_batch_above_the_form_boundary_equals_worlds_alone(torch, rb, tile):
     """18 worlds, 18.6 M cells in all (25-bit batch keys, the large sort form), two steps; every
-    world equals itself stepped alone (1 M cells or fewer: the small form), field by field."""
+    world equals itself stepped alone (1 M cells or fewer: the small form), field by field.  The
+    hydraulic sub-iterations run as the marching kernel (variant 9: strips of many worlds shared
+    by persistent blocks) or as tiles (variant 4)."""
     stream = torch.cuda.Stream()
     rng = np.random.default_rng(99)
     shapes = [(1024, 1024)] * 12 + [(int(rng.integers(700, 1100)), int(rng.integers(500, 1000))) for _ in range(6)]
@@ -115,7 +118,7 @@ def test_batch_above_the_form_boundary_equals_worlds_alone(torch, rb):
     worlds = []
     b = T.Batch()
     for i, (W, H) in enumerate(shapes):
-        w = T.World(batch_settings(rb), W, H, seed=3000 + i)
+        w = T.World(batch_settings(rb, tile), W, H, seed=3000 + i)
         w.init_synthetic_device(4 + (7 * i) % 29, 1.0 + (i % 3) * 0.5, 500 + i)
         b.add(w, stream)
         worlds.append(w)
@@ -128,10 +131,10 @@ def test_batch_above_the_form_boundary_equals_worlds_alone(torch, rb):
         w.close()
     for i, (W, H) in enumerate(shapes):
         assert T.lib().tecto_sort_wide_pass(W * H) == 0
-        a = T.World(batch_settings(rb), W, H, seed=3000 + i)
+        a = T.World(batch_settings(rb, tile), W, H, seed=3000 + i)
         a.init_synthetic_device(4 + (7 * i) % 29, 1.0 + (i % 3) * 0.5, 500 + i)
         if i < 2:
-            ow = O.OracleWorld(batch_settings(rb), a.download(T.FIELD_HEIGHT), a.download(T.FIELD_PLATE_ID),
+            ow = O.OracleWorld(batch_settings(rb, tile), a.download(T.FIELD_HEIGHT), a.download(T.FIELD_PLATE_ID),
                                a.plates(), 3000 + i)
         a.step(2, stream)
         stream.synchronize()
@@ -150,8 +153,10 @@ def test_batch_above_the_form_boundary_equals_worlds_alone(torch, rb):
 
 def test_8192_world_one_step_matches_oracle(torch):
     """The stress configuration: 8192^2 (67 M cells, 26-bit keys), 64 plates, velocities in
-    [-2, 2], 8-connected CCL on every step; one step against the oracle."""
+    [-2, 2], 8-connected CCL on every step; one step against the oracle, with the marching
+    hydraulic kernel (the autotuner's choice for this size)."""
     s = T.baseline_settings()
+    s.step.hydraulicTile = 9
     s.sim.iterationsForCCL = 1
     s.step.cclConnectivity = T.CCL_8
     W = H = 8192
