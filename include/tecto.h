@@ -143,7 +143,8 @@ typedef struct tecto_step_settings {
     int thermalTile;          /* 0 = autotuner's choice, else 4; 1: 64x32 tiles / 1024 threads, up to 5
                                  iterations per launch; 2: 64x16 / 512, 2 blocks per SM, up to 4;
                                  3: 64x16 / 768, 2 blocks per SM, up to 3; 4: 64x16 / 512, 3 blocks
-                                 per SM, up to 2 */
+                                 per SM, up to 2; 5: column strips of up to 124 cells marched down
+                                 8 rows at a time by a block of 512 threads, one iteration per launch */
     int plateDynamics;        /* TECTO_PLATE_DYNAMICS_*: 0 fixed plate velocities (the benchmark), 1 the
                                  reference's applyPlateMovementChanges after every step */
     int platePolicy;          /* TECTO_PLATE_RELABEL | TECTO_PLATE_MERGE bits, 0 = neither */
@@ -428,10 +429,10 @@ int tecto_batch_phase_thermal(tecto_batch *batch, int iterations, tecto_stream_t
 typedef struct tecto_tuning {
     int hydraulicTile;       /* chosen variant, 1..9 */
     int sortRadixBits;       /* chosen digit width, 8..11 */
-    int thermalTile;         /* chosen variant, 1..4 */
+    int thermalTile;         /* chosen variant, 1..5 */
     float hydraulic_ms[9];   /* one hydraulic sub-iteration with variant 1..9 */
     float sort_ms[4];        /* the collision sort with 8..11-bit digits */
-    float thermal_ms[4];     /* ten thermal iterations with variant 1..4 */
+    float thermal_ms[5];     /* ten thermal iterations with variant 1..5 */
 } tecto_tuning;
 int tecto_autotune(const tecto_settings *settings, const int *widths, const int *heights, int count,
                    tecto_stream_t stream, tecto_tuning *out);

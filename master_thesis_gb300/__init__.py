@@ -184,7 +184,7 @@ class Tuning(C.Structure):
     """tecto_tuning: the autotuner's choice and the per-candidate timings."""
     _fields_ = [
         ("hydraulicTile", C.c_int), ("sortRadixBits", C.c_int), ("thermalTile", C.c_int),
-        ("hydraulic_ms", C.c_float * 9), ("sort_ms", C.c_float * 4), ("thermal_ms", C.c_float * 4),
+        ("hydraulic_ms", C.c_float * 9), ("sort_ms", C.c_float * 4), ("thermal_ms", C.c_float * 5),
     ]
 
     def as_dict(self) -> dict:

@@ -39,7 +39,7 @@ void build_tiles(const Batch &b, int kind, std::vector<uint2> &out)
 void build_strips(const Batch &b, std::vector<uint4> &out, unsigned long long *rows)
 {
     out.clear();
-    const int inner = b.hydro_variant == kHydroMarchVariant ? kMarchInner : kStripInner;
+    const int inner = b.hydro_variant == kHydroStripVariant ? kStripInner : kMarchInner;
     unsigned long long r = 0;
     for (size_t wi = 0; wi < b.members.size(); ++wi) {
         const tecto_world *w = b.members[wi];

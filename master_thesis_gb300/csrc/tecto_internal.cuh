@@ -343,11 +343,12 @@ constexpr int kHydroStripVariant = 8;            // marching column strips in re
 constexpr int kHydroMarchVariant = 9;            // marching row chunks in shared memory (fused path only)
 constexpr int kStripInner = 56;                  // interior columns of one register strip (64 with the halo)
 constexpr int kMarchInner = 120;                 // interior columns of one shared-memory strip (128 with it)
-// the strip table of a batch: every member's columns cut into strips of kMarchInner columns for
-// kHydroMarchVariant, of kStripInner otherwise
+// the strip table of a batch: every member's columns cut into strips of kStripInner columns for
+// kHydroStripVariant, of kMarchInner otherwise (the marching hydraulic and thermal kernels)
 void build_strips(const Batch &b, std::vector<uint4> &out, unsigned long long *rows);
-constexpr int kThermalVariantCount = 4;
+constexpr int kThermalVariantCount = 5;
 constexpr int kDefaultThermalVariant = 4;        // 64 x 16 cells, 512 threads, 2 iterations per launch
+constexpr int kThermalMarchVariant = 5;          // marching row chunks down column strips, one iteration per launch
 int thermal_variant_for(const tecto_settings &s);  // 0 when the settings leave the choice open
 
 // Autotuner cache (tecto_tune.cu): best hydraulic tile variant and sort digit width for a batch

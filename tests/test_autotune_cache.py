@@ -41,7 +41,7 @@ def test_later_record_replaces():
 
 @pytest.mark.parametrize("args", [(0, 1 << 20, 1, 0, 8, 1), (0, 1 << 20, 1, 10, 8, 1), (0, 1 << 20, 1, 4, 7, 1),
                                   (0, 1 << 20, 1, 4, 12, 1), (0, 0, 1, 4, 8, 1), (0, 1 << 20, 0, 4, 8, 1),
-                                  (-1, 1 << 20, 1, 4, 8, 1), (0, 1 << 20, 1, 4, 8, 0), (0, 1 << 20, 1, 4, 8, 5)])
+                                  (-1, 1 << 20, 1, 4, 8, 1), (0, 1 << 20, 1, 4, 8, 0), (0, 1 << 20, 1, 4, 8, 6)])
 def test_invalid_records_rejected(args):
     with pytest.raises(T.TectoError):
         T.autotune_record(*args)

@@ -143,7 +143,7 @@ def test_hydraulic_tile_variants_match_oracle(tile, W, H, dt):
     w.check()
 
 
-@pytest.mark.parametrize("tile", [1, 2, 3, 4])
+@pytest.mark.parametrize("tile", [1, 2, 3, 4, 5])
 @pytest.mark.parametrize("W,H,iters", [(100, 60, 7), (33, 17, 5), (300, 200, 10), (128, 96, 3)])
 def test_thermal_tile_variants_match_oracle(tile, W, H, iters):
     """Every thermal tile shape and per-launch iteration split gives the oracle's result."""

@@ -110,7 +110,7 @@ def test_world_autotune_keeps_results(stream):
     for f in FIELDS:
         np.testing.assert_array_equal(w.download(f), plain.download(f), err_msg=f"field {f}")
     assert T.autotune_lookup(0, W * H, 1) == (t.hydraulicTile, t.sortRadixBits, t.thermalTile)
-    assert 1 <= t.thermalTile <= 4 and t.thermal_ms[t.thermalTile - 1] == min(t.thermal_ms)
+    assert 1 <= t.thermalTile <= 5 and t.thermal_ms[t.thermalTile - 1] == min(t.thermal_ms)
 
 
 def test_shape_autotune_and_batch_autotune(stream):
