@@ -22,32 +22,43 @@ __device__ __forceinline__ void *field_base(const WorldDev &wd, int field, int c
     }
 }
 
-// Grid (blocks, worlds): world blockIdx.y's cells, grid-stride; the packed buffer holds world b's
-// elements from its virtual base on.  T is the element type (a 16-byte flux cell, 4-byte scalars).
-template <typename T, bool TO_WORLD>
-__global__ __launch_bounds__(256) void k_pack(const WorldDev *worlds, int field, int cur_h, int cur_wsf, int cur_id,
-                                              T *packed)
-{
-    const WorldDev &wd = worlds[blockIdx.y];
-    T *fld = reinterpret_cast<T *>(field_base(wd, field, cur_h, cur_wsf, cur_id));
-    T *pk = packed + wd.vbase;
-    const uint32_t n = wd.N;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        if (TO_WORLD) fld[i] = pk[i];
-        else pk[i] = fld[i];
-    }
-}
+// The packed buffer holds the worlds' elements in batch order, world w's from its virtual base
+// vbase[w] on.  Each block copies kPackSpan consecutive virtual cells, 8 independent elements per
+// thread, between the packed buffer and the fields of the one or few worlds they belong to (found
+// by a binary search of the bases).  T is the element type (a 16-byte flux cell, 4-byte scalars,
+// plate-id bytes).
+constexpr int kPackThreads = 256;
+constexpr int kPackSpan = kPackThreads * 8;
 
-template <bool TO_WORLD>
-__global__ __launch_bounds__(256) void k_pack_bytes(const WorldDev *worlds, int cur_id, uint8_t *packed)
+template <typename T, bool TO_WORLD>
+__global__ __launch_bounds__(kPackThreads) void k_pack(const WorldDev *worlds, const uint32_t *vbase, int nworlds,
+                                                       int field, int cur_h, int cur_wsf, int cur_id, T *packed)
 {
-    const WorldDev &wd = worlds[blockIdx.y];
-    uint8_t *fld = wd.id[cur_id];
-    uint8_t *pk = packed + wd.vbase;
-    const uint32_t n = wd.N;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        if (TO_WORLD) fld[i] = pk[i];
-        else pk[i] = fld[i];
+    __shared__ int s_first;
+    const uint32_t b0 = blockIdx.x * (uint32_t)kPackSpan;
+    const uint32_t b1 = min(b0 + (uint32_t)kPackSpan, vbase[nworlds]);
+    if (threadIdx.x == 0) {  // the last world whose base is <= b0
+        int lo = 0, hi = nworlds - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (vbase[mid] <= b0) lo = mid;
+            else hi = mid - 1;
+        }
+        s_first = lo;
+    }
+    __syncthreads();
+    for (int w = s_first; w < nworlds && vbase[w] < b1; ++w) {
+        const WorldDev &wd = worlds[w];
+        T *fld = reinterpret_cast<T *>(field_base(wd, field, cur_h, cur_wsf, cur_id));
+        const uint32_t vb = vbase[w], lo = max(b0, vb), hi = min(b1, vbase[w + 1]);
+#pragma unroll
+        for (int k = 0; k < kPackSpan / kPackThreads; ++k) {
+            const uint32_t i = lo + (uint32_t)(k * kPackThreads) + threadIdx.x;
+            if (i < hi) {
+                if (TO_WORLD) fld[i - vb] = packed[i];
+                else packed[i] = fld[i - vb];
+            }
+        }
     }
 }
 
@@ -69,23 +80,20 @@ size_t field_elem(int field)
 int launch_pack(Batch &b, int field, void *buf, bool to_world, cudaStream_t st)
 {
     const size_t esz = field_elem(field);
-    size_t maxn = 0;
-    for (const tecto_world *w : b.members) maxn = std::max(maxn, w->N);
-    const dim3 grid((unsigned)std::min<size_t>((maxn + 1023) / 1024, 1024), (unsigned)b.members.size());
+    const unsigned grid = (unsigned)((b.total + kPackSpan - 1) / kPackSpan);
+    const int n = (int)b.members.size();
+    if (grid == 0) return TECTO_OK;
+#define TECTO_PACK(T)                                                                                               \
+    (to_world ? k_pack<T, true><<<grid, kPackThreads, 0, st>>>(b.d_worlds, b.d_vbase, n, field, b.cur_h, b.cur_wsf, \
+                                                               b.cur_id, (T *)buf)                                  \
+              : k_pack<T, false><<<grid, kPackThreads, 0, st>>>(b.d_worlds, b.d_vbase, n, field, b.cur_h,          \
+                                                                b.cur_wsf, b.cur_id, (T *)buf))
     switch (esz) {
-        case 16:
-            if (to_world) k_pack<float4, true><<<grid, 256, 0, st>>>(b.d_worlds, field, b.cur_h, b.cur_wsf, b.cur_id, (float4 *)buf);
-            else k_pack<float4, false><<<grid, 256, 0, st>>>(b.d_worlds, field, b.cur_h, b.cur_wsf, b.cur_id, (float4 *)buf);
-            break;
-        case 4:
-            if (to_world) k_pack<uint32_t, true><<<grid, 256, 0, st>>>(b.d_worlds, field, b.cur_h, b.cur_wsf, b.cur_id, (uint32_t *)buf);
-            else k_pack<uint32_t, false><<<grid, 256, 0, st>>>(b.d_worlds, field, b.cur_h, b.cur_wsf, b.cur_id, (uint32_t *)buf);
-            break;
-        default:
-            if (to_world) k_pack_bytes<true><<<grid, 256, 0, st>>>(b.d_worlds, b.cur_id, (uint8_t *)buf);
-            else k_pack_bytes<false><<<grid, 256, 0, st>>>(b.d_worlds, b.cur_id, (uint8_t *)buf);
-            break;
+        case 16: TECTO_PACK(float4); break;
+        case 4: TECTO_PACK(uint32_t); break;
+        default: TECTO_PACK(uint8_t); break;
     }
+#undef TECTO_PACK
     TECTO_CUDA(cudaGetLastError());
     b.launches += 1;
     return TECTO_OK;
