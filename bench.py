@@ -168,6 +168,16 @@ def dist_setup():
     return ws, rank, local
 
 
+def workload_config():
+    """The `config` both arms print for the headline workload (identical in both lines); what each
+    arm ran it on goes in the arm's own keys."""
+    cells = sum(W * H for W, H, *_ in mixed_worlds())
+    return {"workload": f"batched mixed-size worlds: {N_WORLDS} worlds, sides log-uniform 128..1024 (half square, "
+                        "half 2:1), plates 4..32, per-world seeds, benchmark physics, one step = every world advanced "
+                        "one step",
+            "worlds": N_WORLDS, "cells": cells}
+
+
 def mixed_worlds(n=N_WORLDS, seed=SHAPE_SEED):
     """(W, H, plates, gen_seed, world_seed) of the mixed-size batch: side s log-uniform on
     [128, 1024]; even entries s x s, odd entries s x s/2; plates uniform on 4..32."""
@@ -251,9 +261,8 @@ def run_reference(args, ws, rank):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded Voronoi worlds, benchmark physics)", "impl": "reference",
-        "config": {"workload": f"batched mixed-size worlds ({N_WORLDS} worlds, sides log-uniform 128..1024, "
-                               "half square / half 2:1, plates 4..32), benchmark physics",
-                   "worlds": N_WORLDS, "parallelism": "host threads"},
+        "config": workload_config(),
+        "arm": {"parallelism": "host threads", "implementation": "the oracle's C restatement of the reference step"},
         "cpu_baseline": {"value": rate, "unit": "cell-updates/s", "cores": cores, "kind": "port",
                          "sample": f"{worlds} world-steps of the mixed-size batch ({cells} cell-updates, "
                                    f"{secs:.1f} s of stepping) on {cores} OpenMP threads"},
@@ -522,13 +531,12 @@ def run_engine(args, ws, rank, local):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded Voronoi worlds, benchmark physics)",
-            "config": {"workload": f"batched mixed-size worlds: {N_WORLDS} worlds, sides log-uniform 128..1024 "
-                                   "(half square, half 2:1), plates 4..32, per-world seeds; one launch per phase "
-                                   "over all worlds, one CUDA-graph replay per step",
-                       "worlds": N_WORLDS, "cells": total, "parallelism": f"replicas x{ws}",
-                       "tuning": tuning.as_dict(),
-                       "l2": f"no flush: the batch state (~{total * 107 / 1e9:.1f} GB) exceeds the 126 MB L2 "
-                             "many times over every step"},
+            "config": workload_config(),
+            "arm": {"parallelism": f"replicas x{ws}",
+                    "execution": "one launch per phase over all worlds, one CUDA-graph replay per step",
+                    "cells_per_rank": total, "tuning": tuning.as_dict(),
+                    "l2": f"no flush: the batch state (~{total * 107 / 1e9:.1f} GB) exceeds the 126 MB L2 "
+                          "many times over every step"},
             "gpu_launches": int(launches),
             "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},

@@ -153,3 +153,20 @@ def test_rooflines_from_the_committed_profiles():
     assert 0 < r["frac"] < 1
     assert bench.issue_roofline(None, 1, 1.0, 2070.0, 152) is None
     assert bench.issue_roofline(ipc, 1, 1.0, None, 152) is None
+
+
+def test_reference_arm_prints_the_engine_arms_config(capsys):
+    """Both arms of bench.py print the same `config` for the headline workload, so the two lines
+    compare as one workload; the reference arm's line is complete without a GPU."""
+    import json
+    import types
+
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    args = types.SimpleNamespace(steps=1, warmup=1, gpus=1)
+    bench.run_reference(args, 1, 0)
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["config"] == bench.workload_config()
+    assert line["impl"] == "reference" and line["value"] > 0 and line["higher_is_better"] is True
+    assert line["cpu_baseline"]["kind"] == "port" and line["e2e"]["value"] == line["value"]
