@@ -138,6 +138,27 @@ def test_server_continuous_batching_matches_one_at_a_time(stream):
     sv.close()
 
 
+def test_size_aware_admission_on_the_gpu(stream):
+    """Two heavy requests (2^20 cells) and light ones arriving together: the heavy ones run one
+    after the other in arrival order while the light ones ride along, and every request's world
+    equals the one-at-a-time path's."""
+    reqs = [T.Request(width=1024, height=1024, plates=8, steps=3, velRange=1.0, genSeed=700, worldSeed=7000,
+                      arrival_s=0.0),
+            T.Request(width=2048, height=512, plates=6, steps=2, velRange=1.0, genSeed=701, worldSeed=7001,
+                      arrival_s=0.0)]
+    reqs += [T.Request(width=96, height=64, plates=5, steps=2 + i % 3, velRange=1.0, genSeed=710 + i,
+                       worldSeed=7100 + i, arrival_s=0.0) for i in range(6)]
+    sv = T.Server(settings(), 3 * T.world_bytes(2048, 512))
+    res_c, st_c = sv.run_trace(reqs, stream)
+    res_s, _ = sv.run_trace_sequential(reqs, stream)
+    assert st_c.completed == 8
+    assert res_c[1].admit_s >= res_c[0].finish_s                 # heavy requests one at a time
+    assert all(r.admit_s < res_c[0].finish_s for r in res_c[2:])  # the light ones ride along
+    for i, (a, b) in enumerate(zip(res_c, res_s)):
+        assert a.status == b.status == 0 and a.height_checksum == b.height_checksum, f"request {i}"
+    sv.close()
+
+
 def test_live_serving_matches_the_trace_replay(stream):
     """Requests submitted one by one while earlier ones are mid-flight, ticks driven by the caller:
     every ticket's final world equals the trace replay's and the one-at-a-time path's."""
