@@ -475,30 +475,34 @@ def run_engine(args, ws, rank, local):
               for f in up_fields}]
     outs = [{f: torch.empty_like(hosts[0][f]).pin_memory() for f in down_fields}]
 
-    copy = torch.cuda.Stream()
-    cs = copy.cuda_stream
+    up_copy, down_copy = torch.cuda.Stream(), torch.cuda.Stream()  # separate copy engines
+    us, ds = up_copy.cuda_stream, down_copy.cuda_stream
 
     def e2e_run(nsteps):
-        # every step: its inputs copied up (one packed buffer per field, staged on a copy stream while
-        # the previous step computes, then scattered into the worlds), the step, its results gathered
-        # and copied down on the copy stream while the next step computes
+        # every step: its inputs copied up (one packed buffer per field, staged on the upload stream
+        # two steps ahead into the batch's double staging buffers, then scattered into the worlds),
+        # the step, its results gathered and copied down on the download stream while the next step
+        # computes
         def stage():
             for f, t in hosts[0].items():
                 T.check(L.tecto_batch_stage_upload_async(batch.ptr, f, t.data_ptr(), t.numel() * t.element_size(),
-                                                         cs), "stage")
+                                                         us), "stage")
         stage()
+        if nsteps > 1:
+            stage()
         for k in range(nsteps):
             for f in hosts[0]:
                 T.check(L.tecto_batch_commit_upload(batch.ptr, f, sp), "commit")
-            if k + 1 < nsteps:
+            if k + 2 < nsteps:
                 stage()
             batch.step(1, stream)
             for f, t in outs[0].items():
                 T.check(L.tecto_batch_gather_download(batch.ptr, f, sp), "gather")
                 T.check(L.tecto_batch_fetch_download_async(batch.ptr, f, t.data_ptr(), t.numel() * t.element_size(),
-                                                           cs), "fetch")
+                                                           ds), "fetch")
         stream.synchronize()
-        copy.synchronize()
+        up_copy.synchronize()
+        down_copy.synchronize()
 
     e2e_run(2)
     e2e_steps = max(10, args.steps)  # the headline's step count: the pipeline's fill and drain amortise alike

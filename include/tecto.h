@@ -399,9 +399,14 @@ int tecto_batch_download_async(tecto_batch *batch, int field, void *host, size_t
 /* The same split in two so that copies overlap compute: stage_upload copies a packed field into a
  * staging buffer of the batch on copy_stream, commit_upload scatters it into the worlds on the
  * compute stream (after the copy); gather_download collects a field on the compute stream,
- * fetch_download copies it to the host on copy_stream (after the gather).  Events inside the batch
- * order the two streams: a stage waits for the previous commit of that field, a gather for the
- * previous fetch.  The host buffers must stay valid until copy_stream has passed the copy. */
+ * fetch_download copies it to the host on copy_stream (after the gather).  Each field has two
+ * staging buffers in each direction, used in turn, so a stage may run up to two commits ahead (the
+ * copy for step k+2 overlaps step k+1 and part of step k) and a gather up to two fetches ahead;
+ * one more is TECTO_ERR_INVALID, and so is a commit with nothing staged or a fetch with nothing
+ * gathered.  Events inside the batch order the streams: a stage waits for the commit that last read
+ * its buffer, a gather for the fetch that last read its buffer.  Uploads and downloads may use
+ * different copy streams (separate copy engines).  The host buffers must stay valid until the copy
+ * stream has passed the copy. */
 int tecto_batch_stage_upload_async(tecto_batch *batch, int field, const void *host, size_t bytes,
                                    tecto_stream_t copy_stream);
 int tecto_batch_commit_upload(tecto_batch *batch, int field, tecto_stream_t stream);

@@ -140,15 +140,19 @@ void batch_release(Batch &b)
     if (b.arena) cudaFree(b.arena);
     if (b.stage) cudaFree(b.stage);
     for (int f = 0; f < 6; ++f) {
-        if (b.up_stage[f]) cudaFree(b.up_stage[f]);
-        if (b.down_stage[f]) cudaFree(b.down_stage[f]);
-        b.up_stage[f] = b.down_stage[f] = nullptr;
-        b.up_bytes[f] = b.down_bytes[f] = 0;
-        cudaEvent_t *evs[4] = {&b.ev_up_ready[f], &b.ev_up_free[f], &b.ev_down_ready[f], &b.ev_down_free[f]};
-        for (cudaEvent_t *e : evs) {
-            if (*e) cudaEventDestroy(*e);
-            *e = nullptr;
+        for (int k = 0; k < 2; ++k) {
+            if (b.up_stage[f][k]) cudaFree(b.up_stage[f][k]);
+            if (b.down_stage[f][k]) cudaFree(b.down_stage[f][k]);
+            b.up_stage[f][k] = b.down_stage[f][k] = nullptr;
+            cudaEvent_t *evs[4] = {&b.ev_up_ready[f][k], &b.ev_up_free[f][k], &b.ev_down_ready[f][k],
+                                   &b.ev_down_free[f][k]};
+            for (cudaEvent_t *e : evs) {
+                if (*e) cudaEventDestroy(*e);
+                *e = nullptr;
+            }
         }
+        b.up_bytes[f] = b.down_bytes[f] = 0;
+        b.n_staged[f] = b.n_committed[f] = b.n_gathered[f] = b.n_fetched[f] = 0;
     }
     b.table_arena = nullptr;
     b.arena = nullptr;

@@ -202,11 +202,13 @@ struct Batch {
     int upref_final = 0;                     // jfa[] half holding the last step's seeds
     void *stage = nullptr;                   // packed host transfers: one field of every member
     size_t stage_bytes = 0;
-    // pipelined packed transfers: per field an upload and a download staging buffer, and the events
-    // that order the copy stream against the compute stream
-    void *up_stage[6] = {}, *down_stage[6] = {};
+    // pipelined packed transfers: per field two upload and two download staging buffers, used in
+    // turn, the events that order the copy streams against the compute stream, and how many stages,
+    // commits, gathers and fetches each field has seen (a stage may run up to two commits ahead)
+    void *up_stage[6][2] = {}, *down_stage[6][2] = {};
     size_t up_bytes[6] = {}, down_bytes[6] = {};
-    cudaEvent_t ev_up_ready[6] = {}, ev_up_free[6] = {}, ev_down_ready[6] = {}, ev_down_free[6] = {};
+    cudaEvent_t ev_up_ready[6][2] = {}, ev_up_free[6][2] = {}, ev_down_ready[6][2] = {}, ev_down_free[6][2] = {};
+    uint64_t n_staged[6] = {}, n_committed[6] = {}, n_gathered[6] = {}, n_fetched[6] = {};
     // graphs of one step keyed by (cur_h, cur_wsf, cur_id, ccl)
     cudaGraphExec_t graphs[16] = {};
     bool graph_valid[16] = {};

@@ -119,7 +119,8 @@ int ensure_event(cudaEvent_t *e)
     return TECTO_OK;
 }
 
-// The per-field staging buffer (allocated for the batch's cells) and its two events.
+// The per-field staging buffers (two, allocated for the batch's cells) and their events.  A change
+// of size drops both buffers and restarts the field's counters.
 int pipe_prepare(tecto_batch *batch, int field, size_t bytes, bool up, int *slot_out, cudaStream_t st)
 {
     if (!batch) return TECTO_ERR_INVALID;
@@ -138,18 +139,24 @@ int pipe_prepare(tecto_batch *batch, int field, size_t bytes, bool up, int *slot
         set_error("pipelined transfer: bytes must be the batch's cells times the field's element size");
         return TECTO_ERR_INVALID;
     }
-    void **buf = up ? &b.up_stage[slot] : &b.down_stage[slot];
     size_t *cap = up ? &b.up_bytes[slot] : &b.down_bytes[slot];
     if (*cap != bytes) {
-        TECTO_CUDA(cudaDeviceSynchronize());  // the old buffer may still be in flight on either stream
-        if (*buf) cudaFree(*buf);
-        *buf = nullptr;
+        TECTO_CUDA(cudaDeviceSynchronize());  // the old buffers may still be in flight on any stream
+        for (int k = 0; k < 2; ++k) {
+            void **buf = up ? &b.up_stage[slot][k] : &b.down_stage[slot][k];
+            if (*buf) cudaFree(*buf);
+            *buf = nullptr;
+        }
         *cap = 0;
-        TECTO_CUDA(cudaMalloc(buf, bytes));
+        for (int k = 0; k < 2; ++k) TECTO_CUDA(cudaMalloc(up ? &b.up_stage[slot][k] : &b.down_stage[slot][k], bytes));
         *cap = bytes;
+        if (up) b.n_staged[slot] = b.n_committed[slot] = 0;
+        else b.n_gathered[slot] = b.n_fetched[slot] = 0;
     }
-    if ((rc = ensure_event(up ? &b.ev_up_ready[slot] : &b.ev_down_ready[slot])) != TECTO_OK) return rc;
-    if ((rc = ensure_event(up ? &b.ev_up_free[slot] : &b.ev_down_free[slot])) != TECTO_OK) return rc;
+    for (int k = 0; k < 2; ++k) {
+        if ((rc = ensure_event(up ? &b.ev_up_ready[slot][k] : &b.ev_down_ready[slot][k])) != TECTO_OK) return rc;
+        if ((rc = ensure_event(up ? &b.ev_up_free[slot][k] : &b.ev_down_free[slot][k])) != TECTO_OK) return rc;
+    }
     *slot_out = slot;
     return TECTO_OK;
 }
@@ -211,9 +218,15 @@ int tecto_batch_stage_upload_async(tecto_batch *batch, int field, const void *ho
     int rc = pipe_prepare(batch, field, bytes, true, &slot, cs);
     if (rc != TECTO_OK) return rc;
     Batch &b = batch->b;
-    TECTO_CUDA(cudaStreamWaitEvent(cs, b.ev_up_free[slot], 0));  // the last commit has read the buffer
-    TECTO_CUDA(cudaMemcpyAsync(b.up_stage[slot], host, bytes, cudaMemcpyHostToDevice, cs));
-    TECTO_CUDA(cudaEventRecord(b.ev_up_ready[slot], cs));
+    if (b.n_staged[slot] >= b.n_committed[slot] + 2) {
+        set_error("tecto_batch_stage_upload_async: two stages of this field already wait for their commits");
+        return TECTO_ERR_INVALID;
+    }
+    const int k = (int)(b.n_staged[slot] & 1);
+    TECTO_CUDA(cudaStreamWaitEvent(cs, b.ev_up_free[slot][k], 0));  // the commit that last read this buffer
+    TECTO_CUDA(cudaMemcpyAsync(b.up_stage[slot][k], host, bytes, cudaMemcpyHostToDevice, cs));
+    TECTO_CUDA(cudaEventRecord(b.ev_up_ready[slot][k], cs));
+    b.n_staged[slot] += 1;
     return TECTO_OK;
 }
 
@@ -222,16 +235,18 @@ int tecto_batch_commit_upload(tecto_batch *batch, int field, tecto_stream_t stre
     if (!batch) return TECTO_ERR_INVALID;
     Batch &b = batch->b;
     const int slot = field_slot(field);
-    if (slot < 0 || !b.up_stage[slot] || b.up_bytes[slot] != b.total * field_elem(field)) {
+    if (slot < 0 || b.up_bytes[slot] != b.total * field_elem(field) || b.n_committed[slot] >= b.n_staged[slot]) {
         set_error("tecto_batch_commit_upload: nothing staged for this field and batch");
         return TECTO_ERR_INVALID;
     }
     const cudaStream_t st = (cudaStream_t)stream;
     int rc = batch_prepare(b, st);
     if (rc != TECTO_OK) return rc;
-    TECTO_CUDA(cudaStreamWaitEvent(st, b.ev_up_ready[slot], 0));
-    if ((rc = launch_pack(b, field, b.up_stage[slot], true, st)) != TECTO_OK) return rc;
-    TECTO_CUDA(cudaEventRecord(b.ev_up_free[slot], st));
+    const int k = (int)(b.n_committed[slot] & 1);
+    TECTO_CUDA(cudaStreamWaitEvent(st, b.ev_up_ready[slot][k], 0));
+    if ((rc = launch_pack(b, field, b.up_stage[slot][k], true, st)) != TECTO_OK) return rc;
+    TECTO_CUDA(cudaEventRecord(b.ev_up_free[slot][k], st));
+    b.n_committed[slot] += 1;
     return TECTO_OK;
 }
 
@@ -244,9 +259,15 @@ int tecto_batch_gather_download(tecto_batch *batch, int field, tecto_stream_t st
     int rc = pipe_prepare(batch, field, bytes, false, &slot, st);
     if (rc != TECTO_OK) return rc;
     Batch &b = batch->b;
-    TECTO_CUDA(cudaStreamWaitEvent(st, b.ev_down_free[slot], 0));  // the last fetch has read the buffer
-    if ((rc = launch_pack(b, field, b.down_stage[slot], false, st)) != TECTO_OK) return rc;
-    TECTO_CUDA(cudaEventRecord(b.ev_down_ready[slot], st));
+    if (b.n_gathered[slot] >= b.n_fetched[slot] + 2) {
+        set_error("tecto_batch_gather_download: two gathers of this field already wait for their fetches");
+        return TECTO_ERR_INVALID;
+    }
+    const int k = (int)(b.n_gathered[slot] & 1);
+    TECTO_CUDA(cudaStreamWaitEvent(st, b.ev_down_free[slot][k], 0));  // the fetch that last read this buffer
+    if ((rc = launch_pack(b, field, b.down_stage[slot][k], false, st)) != TECTO_OK) return rc;
+    TECTO_CUDA(cudaEventRecord(b.ev_down_ready[slot][k], st));
+    b.n_gathered[slot] += 1;
     return TECTO_OK;
 }
 
@@ -256,14 +277,16 @@ int tecto_batch_fetch_download_async(tecto_batch *batch, int field, void *host, 
     if (!batch || !host) return TECTO_ERR_INVALID;
     Batch &b = batch->b;
     const int slot = field_slot(field);
-    if (slot < 0 || !b.down_stage[slot] || bytes != b.down_bytes[slot]) {
+    if (slot < 0 || bytes != b.down_bytes[slot] || b.n_fetched[slot] >= b.n_gathered[slot]) {
         set_error("tecto_batch_fetch_download_async: no gathered field of this size");
         return TECTO_ERR_INVALID;
     }
     const cudaStream_t cs = (cudaStream_t)copy_stream;
-    TECTO_CUDA(cudaStreamWaitEvent(cs, b.ev_down_ready[slot], 0));
-    TECTO_CUDA(cudaMemcpyAsync(host, b.down_stage[slot], bytes, cudaMemcpyDeviceToHost, cs));
-    TECTO_CUDA(cudaEventRecord(b.ev_down_free[slot], cs));
+    const int k = (int)(b.n_fetched[slot] & 1);
+    TECTO_CUDA(cudaStreamWaitEvent(cs, b.ev_down_ready[slot][k], 0));
+    TECTO_CUDA(cudaMemcpyAsync(host, b.down_stage[slot][k], bytes, cudaMemcpyDeviceToHost, cs));
+    TECTO_CUDA(cudaEventRecord(b.ev_down_free[slot][k], cs));
+    b.n_fetched[slot] += 1;
     return TECTO_OK;
 }
 

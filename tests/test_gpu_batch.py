@@ -302,3 +302,62 @@ def test_pipelined_transfers_equal_plain_ones(stream):
         np.testing.assert_array_equal(wa.download(T.FIELD_WATER), wb.download(T.FIELD_WATER))
     ba.close()
     bb.close()
+
+
+def test_pipelined_transfers_two_steps_ahead(stream):
+    """Each field's two staging buffers per direction let uploads run two steps ahead of their
+    commits, on their own copy stream, with downloads on another: five steps of new inputs give the
+    same results as the single-stream packed calls.  A third stage without a commit, a commit with
+    nothing staged and a fetch with nothing gathered are refused."""
+    torch = pytest.importorskip("torch")
+    s = settings()
+    a = [make(sp, s) for sp in SPECS]
+    b = [make(sp, s) for sp in SPECS]
+    ba, bb = T.Batch(), T.Batch()
+    for w in a:
+        ba.add(w, stream)
+    for w in b:
+        bb.add(w, stream)
+    L = T.lib()
+    up, down = torch.cuda.Stream(), torch.cuda.Stream()
+    us, ds, ss = up.cuda_stream, down.cuda_stream, stream.cuda_stream
+    total = int(bb.offsets()[-1])
+    rng = np.random.default_rng(5)
+    n = 5
+    inputs = [torch.from_numpy((rng.random(total) * 2).astype(np.float32)).pin_memory() for _ in range(n)]
+    ids_in = [torch.from_numpy(rng.integers(0, 6, total).astype(np.uint8)).pin_memory() for _ in range(n)]
+    outs_a = [torch.empty(total, dtype=torch.float32).pin_memory() for _ in range(n)]
+    outs_b = [torch.empty(total, dtype=torch.float32).pin_memory() for _ in range(n)]
+    nb = total * 4
+
+    def stage(k):
+        T.check(L.tecto_batch_stage_upload_async(bb.ptr, T.FIELD_WATER, inputs[k].data_ptr(), nb, us), "stage")
+        T.check(L.tecto_batch_stage_upload_async(bb.ptr, T.FIELD_PLATE_ID, ids_in[k].data_ptr(), total, us), "stage")
+
+    stage(0)
+    stage(1)
+    assert L.tecto_batch_stage_upload_async(bb.ptr, T.FIELD_WATER, inputs[2].data_ptr(), nb, us) == -1  # TECTO_ERR_INVALID
+    for k in range(n):
+        ba.upload_packed_async(T.FIELD_WATER, inputs[k].data_ptr(), nb, stream)
+        ba.upload_packed_async(T.FIELD_PLATE_ID, ids_in[k].data_ptr(), total, stream)
+        ba.step(1, stream)
+        ba.download_packed_async(T.FIELD_HEIGHT, outs_a[k].data_ptr(), nb, stream)
+        T.check(L.tecto_batch_commit_upload(bb.ptr, T.FIELD_WATER, ss), "commit")
+        T.check(L.tecto_batch_commit_upload(bb.ptr, T.FIELD_PLATE_ID, ss), "commit")
+        if k + 2 < n:
+            stage(k + 2)
+        bb.step(1, stream)
+        T.check(L.tecto_batch_gather_download(bb.ptr, T.FIELD_HEIGHT, ss), "gather")
+        T.check(L.tecto_batch_fetch_download_async(bb.ptr, T.FIELD_HEIGHT, outs_b[k].data_ptr(), nb, ds), "fetch")
+    assert L.tecto_batch_commit_upload(bb.ptr, T.FIELD_WATER, ss) == -1  # TECTO_ERR_INVALID
+    assert L.tecto_batch_fetch_download_async(bb.ptr, T.FIELD_HEIGHT, outs_b[0].data_ptr(), nb, ds) == -1  # TECTO_ERR_INVALID
+    stream.synchronize()
+    up.synchronize()
+    down.synchronize()
+    for k in range(n):
+        np.testing.assert_array_equal(outs_a[k].numpy(), outs_b[k].numpy(), err_msg=f"step {k}")
+    for wa, wb in zip(a, b):
+        for f in (T.FIELD_WATER, T.FIELD_PLATE_ID, T.FIELD_HEIGHT):
+            np.testing.assert_array_equal(wa.download(f), wb.download(f))
+    ba.close()
+    bb.close()
