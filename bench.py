@@ -743,7 +743,8 @@ def run_case(args):
     policy2048   the same with plate dynamics, relabel after a CCL on every step, and merges;
     collide2048  three collide phases (advection fused into the sort, winner pick, collision types)
                  of one 2048^2 world, 32 plates, 8-bit sort digits;
-    batch        the mixed-size batch with the default tile and digit width, 4 steps."""
+    batch        the mixed-size batch, 4 steps, with the variants --hydro-tile, --thermal-tile and
+                 --radix-bits (the autotuner's choices of a bench line: `--tuned-from LINE.json`)."""
     import torch
 
     import master_thesis_gb300 as T
@@ -797,7 +798,8 @@ def run_case(args):
         w.check(stream)
     else:
         s.step.hydraulicTile = args.hydro_tile
-        s.step.sortRadixBits = 9
+        s.step.thermalTile = args.thermal_tile
+        s.step.sortRadixBits = args.radix_bits
         b = T.Batch()
         worlds = []
         for W, H, P, gs, wsd in mixed_worlds():
@@ -820,11 +822,18 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=64)
     ap.add_argument("--quick", action="store_true", help="headline only (no plain/served/large-world lines)")
     ap.add_argument("--hydro-tile", type=int, default=4, help="hydraulic variant of the --case captures")
+    ap.add_argument("--thermal-tile", type=int, default=0, help="thermal variant of --case batch (0: the default)")
+    ap.add_argument("--radix-bits", type=int, default=9, help="sort digit width of --case batch")
     ap.add_argument("--case", choices=["erosion2048", "erosion4096", "plain2048", "policy2048", "collide2048",
                                        "collide4096", "batch"],
                     help="a small fixed workload for profilers")
+    ap.add_argument("--tuned-from", default=None,
+                    help="take --hydro-tile / --thermal-tile / --radix-bits from the tuning of a bench JSON line")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.tuned_from:
+        t = json.loads(open(args.tuned_from).read().strip().splitlines()[-1])["arm"]["tuning"]
+        args.hydro_tile, args.thermal_tile, args.radix_bits = t["hydraulicTile"], t["thermalTile"], t["sortRadixBits"]
     ws, rank, local = dist_setup()
     if args.case:
         run_case(args)

@@ -169,14 +169,14 @@ __global__ void k_type_matrix(const WorldDev *worlds, int cooldown, int minSize)
     PairCounts *counts = wd.counts;
     uint8_t *bm = wd.type_bitmap;
     const PairCounts pc = counts[idx];
+    const int *c = pc.c;
+    const uint32_t total = (uint32_t)(c[0] + c[1] + c[2] + c[3] + c[4]);
+    if (total == 0) return;  // no evidence: the counts are zero already
     int *cp = counts[idx].c;
     cp[0] = cp[1] = cp[2] = cp[3] = cp[4] = 0;
-    const int *c = pc.c;
     const uint32_t packed = bm[idx];
     const bool hasType = packed & 1u;
     const int count = (int)((packed >> 4) & 0x0Fu);
-    const uint32_t total = (uint32_t)(c[0] + c[1] + c[2] + c[3] + c[4]);
-    if (total == 0) return;
     if (hasType && count < cooldown) {
         bm[idx] = (uint8_t)((packed & 0x0Fu) | (((uint32_t)(count + 1) & 0x0Fu) << 4));
         return;
