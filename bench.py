@@ -751,6 +751,7 @@ def run_case(args):
 
     stream = torch.cuda.Stream()
     s = T.baseline_settings()
+    s.step.thermalTile = args.thermal_tile
     if args.case == "erosion2048":
         s.step.hydraulicTile = args.hydro_tile
         w = T.World(s, 2048, 2048, seed=1000)
@@ -798,7 +799,6 @@ def run_case(args):
         w.check(stream)
     else:
         s.step.hydraulicTile = args.hydro_tile
-        s.step.thermalTile = args.thermal_tile
         s.step.sortRadixBits = args.radix_bits
         b = T.Batch()
         worlds = []
@@ -822,7 +822,7 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=64)
     ap.add_argument("--quick", action="store_true", help="headline only (no plain/served/large-world lines)")
     ap.add_argument("--hydro-tile", type=int, default=4, help="hydraulic variant of the --case captures")
-    ap.add_argument("--thermal-tile", type=int, default=0, help="thermal variant of --case batch (0: the default)")
+    ap.add_argument("--thermal-tile", type=int, default=0, help="thermal variant of the --case captures (0: the default)")
     ap.add_argument("--radix-bits", type=int, default=9, help="sort digit width of --case batch")
     ap.add_argument("--case", choices=["erosion2048", "erosion4096", "plain2048", "policy2048", "collide2048",
                                        "collide4096", "batch"],
