@@ -31,6 +31,7 @@ def settings(tile=0):
     s.kernel.collisionTypeUpdateCooldown = 2
     s.sim.iterationsForCCL = 3
     s.step.hydraulicTile = tile
+    s.step.thermalTile = 5 if tile == 9 else 0  # the marching kernels together
     return s
 
 
@@ -50,8 +51,8 @@ def assert_same(a: T.World, b: T.World, msg):
 
 @pytest.mark.parametrize("tile", [4, 9])
 def test_batch_equals_alone_with_joins_and_leaves(stream, tile):
-    """Tiles (variant 4) and the marching kernel (variant 9), whose strip table and persistent
-    block ranges are rebuilt at every membership change."""
+    """Tiles (hydraulic variant 4) and the marching kernels (hydraulic 9, thermal 5), whose strip
+    table and persistent block ranges are rebuilt at every membership change."""
     s = settings(tile)
     alone = [make(sp, s) for sp in SPECS]
     mixed = [make(sp, s) for sp in SPECS]

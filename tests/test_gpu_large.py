@@ -101,6 +101,7 @@ def batch_settings(rb, tile=4):
     s.sim.iterationsForCCL = 1
     s.step.sortRadixBits = rb
     s.step.hydraulicTile = tile
+    s.step.thermalTile = 5 if tile == 9 else 4  # the marching kernels together, or the tiles
     return s
 
 
@@ -154,9 +155,10 @@ def test_batch_above_the_form_boundary_equals_worlds_alone(torch, rb, tile):
 def test_8192_world_one_step_matches_oracle(torch):
     """The stress configuration: 8192^2 (67 M cells, 26-bit keys), 64 plates, velocities in
     [-2, 2], 8-connected CCL on every step; one step against the oracle, with the marching
-    hydraulic kernel (the autotuner's choice for this size)."""
+    hydraulic and thermal kernels (the autotuner's choices for this size)."""
     s = T.baseline_settings()
     s.step.hydraulicTile = 9
+    s.step.thermalTile = 5
     s.sim.iterationsForCCL = 1
     s.step.cclConnectivity = T.CCL_8
     W = H = 8192
