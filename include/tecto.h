@@ -626,6 +626,15 @@ int tecto_world_check(tecto_world *world, tecto_stream_t stream);
  * out[i] = a[i] / b[i] computed that way, on device buffers.  Tests compare it bit for bit with
  * the IEEE quotient. */
 int tecto_selftest_div(const float *a, const float *b, float *out, size_t n, tecto_stream_t stream);
+/* The same for the per-lane form the erosion kernels use where every cell has its own divisor:
+ * the quotient from a correctly rounded reciprocal (one Newton-Raphson step from the hardware's
+ * approximation), with the IEEE division outside its safe range. */
+int tecto_selftest_div_var(const float *a, const float *b, float *out, size_t n, tecto_stream_t stream);
+/* Exhaustive self-test of the erosion kernels' reciprocal and square root: for every positive
+ * normal float, whether each equals the correctly rounded result.  bad (device, 512 counters)
+ * receives the mismatches per exponent field: bad[e] for the reciprocal, bad[256 + e] for the
+ * square root. */
+int tecto_selftest_rcp_sqrt(unsigned long long *bad, tecto_stream_t stream);
 const char *tecto_last_error_string(void);
 const char *tecto_version(void);
 

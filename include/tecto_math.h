@@ -30,6 +30,25 @@
 #include <string.h>
 #endif
 
+/* 2/pi; rintf(x * TECTO_TWO_OVER_PI) is the quadrant of the reduction */
+#define TECTO_TWO_OVER_PI 0.6366197466850281f
+
+/* The sine series of the reduced argument r (Taylor coefficients 1/n! with alternating signs). */
+TECTO_HD float tecto_sin_series(float r)
+{
+    const float S3 = -1.6666666666666666e-1f;
+    const float S5 = 8.3333333333333332e-3f;
+    const float S7 = -1.9841269841269841e-4f;
+    const float S9 = 2.7557319223985893e-6f;
+    const float S11 = -2.5052108385441720e-8f;
+    const float r2 = r * r;
+    float ps = fmaf(r2, S11, S9);
+    ps = fmaf(r2, ps, S7);
+    ps = fmaf(r2, ps, S5);
+    ps = fmaf(r2, ps, S3);
+    return fmaf(r * r2, ps, r);
+}
+
 /* The shared core of tecto_sinf and tecto_cosf: the quadrant q of x and the sine and cosine of the
  * reduced argument.  Every step is a fused multiply-add (one rounding), the same on the GPU (FFMA)
  * and on the host (C99 fmaf, correctly rounded), so both sides still agree bit for bit; the
@@ -41,13 +60,8 @@ TECTO_HD void tecto_sincos_core(float x, int *q, float *s, float *c)
     const float C2 = 4.825592041015625e-4f;
     const float C3 = 1.2665987014770508e-6f;
     const float C4 = 9.92093629470503e-10f;
-    const float TWO_OVER_PI = 0.6366197466850281f;
+    const float TWO_OVER_PI = TECTO_TWO_OVER_PI;
     /* Taylor coefficients 1/n! with alternating signs */
-    const float S3 = -1.6666666666666666e-1f;
-    const float S5 = 8.3333333333333332e-3f;
-    const float S7 = -1.9841269841269841e-4f;
-    const float S9 = 2.7557319223985893e-6f;
-    const float S11 = -2.5052108385441720e-8f;
     const float K2 = -0.5f;
     const float K4 = 4.1666666666666664e-2f;
     const float K6 = -1.3888888888888889e-3f;
@@ -60,11 +74,7 @@ TECTO_HD void tecto_sincos_core(float x, int *q, float *s, float *c)
     r = fmaf(-kf, C3, r);
     r = fmaf(-kf, C4, r);
     const float r2 = r * r;
-    float ps = fmaf(r2, S11, S9);
-    ps = fmaf(r2, ps, S7);
-    ps = fmaf(r2, ps, S5);
-    ps = fmaf(r2, ps, S3);
-    *s = fmaf(r * r2, ps, r);
+    *s = tecto_sin_series(r);
     float pc = fmaf(r2, K10, K8);
     pc = fmaf(r2, pc, K6);
     pc = fmaf(r2, pc, K4);

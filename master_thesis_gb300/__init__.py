@@ -302,6 +302,8 @@ def _declare(L: C.CDLL) -> None:
         "tecto_server_poll": ([P, C.c_int, C.POINTER(C.c_int), C.POINTER(RequestResult)], C.c_int),
         "tecto_server_live_stats": ([P, C.POINTER(ServerStats)], C.c_int),
         "tecto_selftest_div": ([P, P, P, C.c_size_t, P], C.c_int),
+        "tecto_selftest_div_var": ([P, P, P, C.c_size_t, P], C.c_int),
+        "tecto_selftest_rcp_sqrt": ([P, P], C.c_int),
         "tecto_png_encode": ([P, C.c_int, C.c_int, C.c_int, P, C.c_size_t, C.POINTER(C.c_size_t)], C.c_int),
         "tecto_plate_palette": ([P], C.c_int),
         "tecto_world_export_png": ([P, C.c_int, C.c_char_p, C.c_float, C.c_float, P], C.c_int),
