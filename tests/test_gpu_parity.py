@@ -159,6 +159,27 @@ def test_thermal_tile_variants_match_oracle(tile, W, H, iters):
     w.check()
 
 
+@pytest.mark.parametrize("tile", [4, 5])
+@pytest.mark.parametrize("angle,amplitude", [(0.0, None), (-0.5, None), (0.5, -0.5)])
+def test_thermal_general_parameters_match_oracle(tile, angle, amplitude):
+    """A threshold below 2^-64 and flows that may be negative (negative threshold or amplitude)
+    take the general forms of the tile and marching kernels: bit for bit the oracle's result."""
+    st, w = make_world("baseline", 100, 60)
+    st.step.thermalTile = tile
+    st.kernel.thermalThresholdAngle = angle
+    if amplitude is not None:
+        st.kernel.thermalErosionAmplitude = amplitude
+    w.set_settings(st)
+    rng = np.random.default_rng(7 + tile)
+    h = (w.download(T.FIELD_HEIGHT) + rng.normal(0, 0.05, (60, 100))).astype(np.float32)
+    w.upload(T.FIELD_HEIGHT, h)
+    w.thermal(3)
+    want = O.thermal(h, 3, st)
+    got = w.download(T.FIELD_HEIGHT)
+    np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
+    w.check()
+
+
 @pytest.mark.parametrize("W,H,steps", [(64, 64, 12), (100, 60, 12), (256, 256, 6)])
 def test_graph_steps_match_oracle(torch_stream, W, H, steps):
     st, w = make_world("baseline", W, H)
