@@ -128,4 +128,10 @@ def test_invalid_arguments_are_rejected_without_touching_a_gpu():
     # the pass form for large sorts starts at 4096 tiles of 4096 keys
     assert L.tecto_sort_wide_pass(4096 * 4096) == 1 and L.tecto_sort_wide_pass(4096 * 4096 - 4096) == 0
     assert L.tecto_sort_wide_pass(4095 * 4096 + 1) == 1
+    # the erosion kernels' arithmetic self-tests check their arguments before any device work
+    assert L.tecto_selftest_div(None, None, None, 0, None) == 0
+    assert L.tecto_selftest_div(None, None, None, 16, None) == -1
+    assert L.tecto_selftest_div_var(None, None, None, 0, None) == 0
+    assert L.tecto_selftest_div_var(None, None, None, 16, None) == -1
+    assert L.tecto_selftest_rcp_sqrt(None, None) == -1
     assert L.tecto_world_destroy(None) == 0
